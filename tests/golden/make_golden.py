@@ -1,0 +1,119 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's own code.
+
+Run in the development container, where the reference tree exists:
+
+    python tests/golden/make_golden.py
+
+It compiles the reference's kernel.c (as produced by its kernel.py) and its vendored
+RANLUXCL header on the CPU (oracle/build_ref.py) and records inputs and outputs:
+
+* ``ranlux_streams.npz``: RANLUXCL uniforms and final 28-word states for luxury levels
+  0-4 and p=124, FP32 and FP64 variants (pyopencl-ranluxcl.cl:384-557, :597-725, :893-920);
+* ``sweep_<case>.npz``: initial paths and seed tables, and after each of two
+  ``metropolis`` launches: paths, accept counts, seed / RANLUX tables, operator means,
+  correlator sums and histogram bins (kernel.c:514-837).
+
+The fixtures hold numbers only (no reference source text).  The plugin used is the
+1D harmonic oscillator V = 0.5*k*x^2 with the virial operator k*x^2
+(FeynSimul/physical_systems/harm_osc.py:46-53), written out in ``CASES`` below.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from oracle import build_ref as br  # noqa: E402
+
+HO = dict(DOF=1, potential="0.5 * 1.0 * x1 * x1",
+          userCode="FLOAT_TYPE sqr(FLOAT_TYPE x){return x*x;}")
+
+BASE = dict(nbrOfWalkers=8, N=16, beta=10.0, S=2, enableOperator=True, enableCorrelator=True,
+            enableBisection=True, enablePathShift=False, enableSingleNodeMove=False,
+            enableBins=True, nbrOfWalkersPerWorkGroup=2, enableParallelizePath=True,
+            enableGlobalPath=True, enableGlobalOldPath=False, enableDouble=False,
+            enableRanlux=False, operators=("1.0 * x1 * x1", "x1"),
+            correlators=("x1", "x1*x1"), operatorRuns=3, metroStepsPerOperatorRun=5,
+            xMin=-3.0, xMax=3.0, binResolutionPerDOF=10)
+
+CASES = {
+    "xorshift_parallel": dict(BASE),
+    "xorshift_parallel_wpg1_s3": dict(BASE, nbrOfWalkers=6, N=32, S=3, nbrOfWalkersPerWorkGroup=1),
+    "xorshift_walker": dict(BASE, enableParallelizePath=False, nbrOfWalkersPerWorkGroup=1),
+    "xorshift_parallel_double": dict(BASE, enableDouble=True),
+    "ranlux_parallel_lux2": dict(BASE, enableRanlux=True, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
+                                 nbrOfWalkersPerWorkGroup=1, nbrOfWalkers=4),
+    "ranlux_walker_lux0": dict(BASE, enableRanlux=True, luxuaryFactor=0, ranluxIntMax=2 ** 31 - 1,
+                               enableParallelizePath=False, nbrOfWalkersPerWorkGroup=1,
+                               nbrOfWalkers=4, S=3),
+    "xorshift_parallel_s1_big": dict(BASE, nbrOfWalkers=4, N=64, S=1, nbrOfWalkersPerWorkGroup=4,
+                                     operatorRuns=2, metroStepsPerOperatorRun=3),
+}
+
+
+def make_ranlux():
+    seeds = np.array([1, 12345, 2 ** 31 - 5, 987654321123, 0xDEADBEEFCAFE], np.uint64)
+    out = {"seeds": seeds}
+    for lux in (0, 1, 2, 3, 4, 124):
+        s32, st = br.ref_ranlux_streams(lux, seeds, 100)
+        s64, _ = br.ref_ranlux_streams(lux, seeds[:2], 40, double=True)
+        st[:, 25] = 0  # padding word, uninitialised in the reference
+        out[f"f32_lux{lux}"] = s32
+        out[f"state_lux{lux}"] = st
+        out[f"f64_lux{lux}"] = s64
+    np.savez_compressed(os.path.join(HERE, "ranlux_streams.npz"), **out)
+
+
+def make_sweep(name, ka):
+    system = types.SimpleNamespace(**HO)
+    r = br.RefKernel(ka, system, np_seed=11)
+    k = r.k
+    rng = np.random.RandomState(5)
+    p0 = (rng.randn(*k._paths.arr.shape) * 0.3).astype(k._paths.arr.dtype)
+    k._paths.arr[...] = p0
+    rec = {"paths0": p0.copy()}
+    if ka["enableRanlux"]:
+        rec["seeds_ranlux"] = k._seeds.arr.copy()
+        rec["group_seeds"] = k._groupSeeds.arr.copy()
+        r.init_ranlux()
+        r.group_init_ranlux()
+        rec["ranlux_tab0"] = k._ranluxcltab.arr.reshape(-1, 28).copy()
+        rec["group_tab0"] = k._groupRanluxcltab.arr.reshape(-1, 28).copy()
+    else:
+        rec["seeds0"] = k._seeds.arr.copy()
+    for it in range(2):
+        r.run()
+        rec[f"paths{it + 1}"] = k._paths.arr.copy()
+        rec[f"accepts{it + 1}"] = k._accepts.arr.copy()
+        rec[f"ops{it + 1}"] = k._operatorValues.arr.copy()
+        rec[f"cor{it + 1}"] = k._correlatorValues.arr.copy()
+        rec[f"bins{it + 1}"] = k._binCounts.arr.ravel().copy()
+        if ka["enableRanlux"]:
+            rec[f"ranlux_tab{it + 1}"] = k._ranluxcltab.arr.reshape(-1, 28).copy()
+            rec[f"group_tab{it + 1}"] = k._groupRanluxcltab.arr.reshape(-1, 28).copy()
+        else:
+            rec[f"seeds{it + 1}"] = k._seeds.arr.copy()
+    for key in list(rec):
+        if "tab" in key:
+            rec[key][:, 25] = 0  # padding word
+    cfg = {k2: v for k2, v in ka.items()}
+    rec["config"] = np.array(repr(cfg))
+    np.savez_compressed(os.path.join(HERE, f"sweep_{name}.npz"), **rec)
+
+
+def main():
+    if not br.reference_available():
+        raise SystemExit("reference tree not present; fixtures are generated where it is")
+    make_ranlux()
+    for name, ka in CASES.items():
+        make_sweep(name, ka)
+        print("wrote", name)
+
+
+if __name__ == "__main__":
+    main()

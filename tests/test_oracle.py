@@ -1,0 +1,91 @@
+"""The CPU oracle restatement against the golden fixtures made from the reference's
+own kernel.c / RANLUXCL (tests/golden/make_golden.py), and, where the reference tree is
+present, against the reference built live (oracle/build_ref.py)."""
+import numpy as np
+import pytest
+
+from golden_cases import load_ranlux, load_sweep, oracle_config, sweep_cases
+from oracle import oracle as orc
+
+
+@pytest.mark.parametrize("lux", [0, 1, 2, 3, 4, 124])
+def test_ranlux_streams_bit_exact(lux):
+    g = load_ranlux()
+    for i, s in enumerate(g["seeds"]):
+        out, st = orc.ranlux_stream(int(s), lux, 100)
+        assert np.array_equal(out.view(np.uint32), g[f"f32_lux{lux}"][i].view(np.uint32))
+        st = st.copy()
+        st[25] = 0
+        assert np.array_equal(st, g[f"state_lux{lux}"][i])
+    for i, s in enumerate(g["seeds"][:2]):
+        out, _ = orc.ranlux_stream(int(s), lux, 40, double=True)
+        assert np.array_equal(out, g[f"f64_lux{lux}"][i])
+
+
+def _masked(t):
+    t = np.array(t).reshape(-1, 28).copy()
+    t[:, 25] = 0
+    return t
+
+
+@pytest.mark.parametrize("case", sweep_cases())
+def test_sweep_matches_reference_golden(case):
+    ka, rec = load_sweep(case)
+    o = orc.OracleSampler(oracle_config(ka, compat=True, accum=0))
+    o.paths[...] = rec["paths0"]
+    if ka["enableRanlux"]:
+        o.ranlux_tab[...] = rec["ranlux_tab0"]
+        o.group_tab[...] = rec["group_tab0"]
+    else:
+        o.seeds[...] = rec["seeds0"]
+    for it in (1, 2):
+        o.run()
+        # seed tables and accept counts: integer, bit-exact
+        if ka["enableRanlux"]:
+            assert np.array_equal(_masked(o.ranlux_tab), rec[f"ranlux_tab{it}"])
+            assert np.array_equal(_masked(o.group_tab), rec[f"group_tab{it}"])
+        else:
+            assert np.array_equal(o.seeds, rec[f"seeds{it}"])
+        assert np.array_equal(o.accepts, rec[f"accepts{it}"])
+        assert np.array_equal(o.bins, rec[f"bins{it}"])
+        # floats: same operations in the same order on IEEE hardware.  libm's
+        # log/sin/exp may differ by an ulp between CPU families, hence the tolerance.
+        np.testing.assert_allclose(o.paths, rec[f"paths{it}"], rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(o.op_means[:rec[f"ops{it}"].size], rec[f"ops{it}"], rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(o.cor_means, rec[f"cor{it}"], rtol=1e-5, atol=1e-5)
+
+
+def test_ranlux_compat_quirks_visible_in_golden():
+    """The reference seeds every per-thread RANLUX state from seeds[0] (kernel.c:155) and
+    its RANLUX integers have zero low bits (kernel.c:206), so the bisection grid never
+    shifts: slices 0, 4, 8, 12 keep their initial values."""
+    ka, rec = load_sweep("ranlux_parallel_lux2")
+    t0 = rec["ranlux_tab0"]
+    assert (t0 == t0[0]).all()
+    seg = 2 ** ka["S"]
+    p0 = rec["paths0"].reshape(ka["nbrOfWalkers"], ka["N"])
+    p2 = rec["paths2"].reshape(ka["nbrOfWalkers"], ka["N"])
+    assert np.array_equal(p0[:, ::seg], p2[:, ::seg])
+    assert not np.array_equal(p0, p2)
+
+
+def test_oracle_against_live_reference():
+    """Where the reference tree exists, rebuild it and compare once more (not a golden)."""
+    from oracle import build_ref as br
+    if not br.reference_available():
+        pytest.skip("reference tree not present")
+    import types
+    from golden_cases import HO
+    ka, _ = load_sweep("xorshift_parallel")
+    r = br.RefKernel(dict(ka, nbrOfWalkers=4, N=32, S=3), types.SimpleNamespace(**HO), np_seed=3)
+    o = orc.OracleSampler(oracle_config(dict(ka, nbrOfWalkers=4, N=32, S=3)))
+    rng = np.random.RandomState(9)
+    p0 = (rng.randn(*r.k._paths.arr.shape) * 0.5).astype(np.float32)
+    r.k._paths.arr[...] = p0
+    o.paths[...] = p0
+    o.seeds[...] = r.k._seeds.arr
+    r.run()
+    o.run()
+    assert np.array_equal(o.seeds, r.k._seeds.arr)
+    assert np.array_equal(o.accepts, r.k._accepts.arr)
+    assert np.array_equal(o.paths, r.k._paths.arr)
