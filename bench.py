@@ -1,0 +1,413 @@
+"""Benchmark: path-node updates/s of the Metropolis-bisection sweep on GB300.
+
+Workload (default ``--config he3``): three He-4 atoms with the LM2M2 pair potential,
+T = 1 K (beta = 1/K), N = 256 slices, bisection level S = 4, 16384 walkers, RANLUX
+(luxuaryFactor 2), FP32 paths, FP64 operator sums; operators: the virial energy and a
+200-bin pair-distance histogram on 0-20 Angstrom.  Paths start as random equilateral
+triangles of side U(3, 5) Angstrom plus N(0, 0.1 Angstrom) noise (seeded).
+
+A step is one PIMCKernel.run(): operatorRuns x metroStepsPerOperatorRun sweeps of every
+walker in one kernel launch.  A node update is one interior time slice (all DOF)
+resampled by a bisection move, accepted or not: walkers x N/2^S segments x (2^S - 1)
+per sweep.
+
+value: node updates/s with the state resident in HBM (CUDA events around each launch,
+L2 flushed between launches).  e2e: the same through the reference-facing API with host
+buffers: each step copies the paths in from pinned host memory, runs, and reads the
+operator means and the paths back.  cpu_baseline: the oracle's C restatement of the
+reference sweep on the host cores (OpenMP) on a bounded sample of the same workload.
+
+``--impl reference`` times the reference algorithm on the CPU instead (the oracle port,
+every host thread): the reference's OpenCL kernels have no runnable OpenCL platform here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+# ------------------------------------------------------------------ workloads
+def he3_setup(walkers=16384, N=256, S=4, op_runs=5, msteps=10):
+    from feynsimul_gb300.physical_systems.lm2m2 import Lm2m2Cluster
+    sysm = Lm2m2Cluster(3, 1.0)
+    ka = dict(nbrOfWalkers=walkers, N=N, beta=float(sysm.beta), S=S, enableOperator=True,
+              enableCorrelator=False, enableBisection=True, enablePathShift=False,
+              enableSingleNodeMove=False, enableBins=False, nbrOfWalkersPerWorkGroup=1,
+              enableParallelizePath=True, enableGlobalPath=False, enableGlobalOldPath=False,
+              enableDouble=False, enableRanlux=True, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
+              operators=(sysm.energyOp,), operatorRuns=op_runs, metroStepsPerOperatorRun=msteps)
+    extra = dict(histograms=sysm.pairDistanceOps, histRange=(0.0, 20.0), histBins=200)
+    workload = (f"He3 LM2M2 T=1K N={N} S={S} walkers={walkers} RANLUX lux2 fp32 paths, "
+                f"fp64 sums, energy + 200-bin pair-distance histogram")
+    return sysm, ka, extra, workload
+
+
+def ho_setup(walkers=1024, N=128, S=3, op_runs=100, msteps=1):
+    from feynsimul_gb300.physical_systems.harm_osc import HarmOsc
+    sysm = HarmOsc()
+    ka = dict(nbrOfWalkers=walkers, N=N, beta=10.0, S=S, enableOperator=True, enableCorrelator=True,
+              enableBisection=True, enablePathShift=False, enableSingleNodeMove=False, enableBins=False,
+              nbrOfWalkersPerWorkGroup=1, enableParallelizePath=True, enableGlobalPath=False,
+              enableGlobalOldPath=False, enableDouble=False, enableRanlux=False,
+              operators=(sysm.energyOp,), correlators=("x1",), operatorRuns=op_runs,
+              metroStepsPerOperatorRun=msteps)
+    return sysm, ka, {}, f"1D HO beta=10 N={N} S={S} walkers={walkers} xorshift, x^2 and <x(0)x(t)>"
+
+
+def initial_paths(sysm, ka, seed):
+    rng = np.random.RandomState(seed)
+    if hasattr(sysm, "initial_paths"):
+        return sysm.initial_paths(ka["nbrOfWalkers"], ka["N"], rng).astype(np.float32)
+    return np.zeros((ka["nbrOfWalkers"], ka["N"] * sysm.DOF), np.float32)
+
+
+def node_updates_per_run(ka):
+    seg = 2 ** ka["S"]
+    tpw = ka["N"] // seg
+    return ka["nbrOfWalkers"] * tpw * (seg - 1) * ka["operatorRuns"] * ka["metroStepsPerOperatorRun"]
+
+
+# ------------------------------------------------------------------ helpers
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thr = threading.Thread(target=self._read, daemon=True)
+            self.thr.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            return json.load(f)
+    except OSError:
+        return None
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_cpu_rate(sysm, ka, extra, seconds=10.0, walkers=None):
+    """Node updates/s of the oracle's C restatement (the reference algorithm) on the host
+    cores, on a bounded sample: a subset of walkers and fewer sweeps, sized to ~seconds."""
+    from oracle import oracle as orc
+    cores = cpu_cores()
+    W = walkers or max(cores * 4, 64)
+    W = min(W, ka["nbrOfWalkers"])
+
+    def make(sweeps):
+        cfg = orc.OracleConfig(
+            DOF=sysm.DOF, potential=sysm.potential, userCode=sysm.userCode, nbrOfWalkers=W, N=ka["N"],
+            beta=ka["beta"], S=ka["S"], operatorRuns=1, metroStepsPerOperatorRun=sweeps,
+            nbrOfWalkersPerWorkGroup=1, enableParallelizePath=True, enableRanlux=ka["enableRanlux"],
+            luxuaryFactor=ka.get("luxuaryFactor", 2), ranluxIntMax=ka.get("ranluxIntMax", 2 ** 32 - 1),
+            operators=ka["operators"], correlators=ka.get("correlators", ()) or (), compat=False, accum=1,
+            histograms=extra.get("histograms", ()), histRange=extra.get("histRange", (0.0, 1.0)),
+            histBins=extra.get("histBins", 0))
+        o = orc.OracleSampler(cfg, omp_threads=cores)
+        o.paths[...] = initial_paths(sysm, dict(ka, nbrOfWalkers=W), 7)
+        if ka["enableRanlux"]:
+            o.init_ranlux_rows(o.ranlux_tab, (np.uint64(12345) << np.uint64(32)) + np.arange(o.ranlux_tab.shape[0], dtype=np.uint64))
+            o.init_ranlux_rows(o.group_tab, (np.uint64(54321) << np.uint64(32)) + np.arange(o.group_tab.shape[0], dtype=np.uint64))
+        else:
+            rs = np.random.RandomState(1)
+            o.seeds[...] = rs.randint(0, 2 ** 31 - 1, size=o.seeds.shape)
+            o.walker_seeds[...] = rs.randint(0, 2 ** 31 - 1, size=o.walker_seeds.shape)
+        return o, cfg
+
+    o, cfg = make(1)
+    t0 = time.perf_counter()
+    o.run()
+    t1 = time.perf_counter() - t0
+    sweeps = int(max(1, min(2000, seconds / max(t1, 1e-4))))
+    o, cfg = make(sweeps)
+    t0 = time.perf_counter()
+    o.run()
+    dt = time.perf_counter() - t0
+    seg = 2 ** ka["S"]
+    nodes = W * (ka["N"] // seg) * (seg - 1) * sweeps
+    return {"value": nodes / dt, "unit": "node-updates/s", "cores": cores, "kind": "port",
+            "sample": f"{W} walkers x {sweeps} sweeps of the same system ({nodes} node updates, {dt:.1f} s), "
+                      f"oracle C restatement, OpenMP over walkers"}
+
+
+def integrated_autocorr(series):
+    """Sokal automatic windowing (c = 5) of the normalised autocorrelation; series[t, walker]."""
+    x = series - series.mean(axis=0, keepdims=True)
+    n = x.shape[0]
+    if n < 4:
+        return 0.5
+    var = (x * x).mean()
+    if var <= 0:
+        return 0.5
+    tau = 0.5
+    for t in range(1, n // 2):
+        rho = (x[:-t] * x[t:]).mean() / var
+        tau += rho
+        if t >= 5 * tau:
+            break
+    return max(tau, 0.5)
+
+
+# ------------------------------------------------------------------ roofline
+# Algorithmic lane operations per node update (one interior slice, all DOF, resampled by a
+# bisection move), counted from the algorithm, not from the executed code:
+#   RNG    2*DOF uniforms (+ amortised accept / offset draws); RANLUX p = 24 + NSKIP steps of
+#          subtract-with-borrow per 24 uniforms, 3 integer ops each, + 4 ops per output and
+#          4 for the buffered hand-out; xorshift 6 ops per uniform + 2 to convert
+#   BM     per DOF: log, sqrt, sin (1 op each, SFU) + 6 multiplies/adds for the midpoint
+#   V      two potential evaluations per node (old and new path); LM2M2 trimer: 15 ops for
+#          the positions, 3 pairs x (6 ops for r^2 + 35 for the pair potential) = 138;
+#          harmonic oscillator: 3
+# The peak is the issue roof of the SMs: 4 schedulers x 32 lanes x 152 SMs per clock, at
+# the median SM clock sampled during the timed region (one lane op per lane per cycle).
+POT_OPS = {"he3": 138.0, "ho": 3.0}
+
+
+def alg_ops_per_node(config, ka):
+    dof = 6 if config == "he3" else 1
+    seg = 2 ** ka["S"]
+    uni = 2 * dof + 2.0 / (seg - 1)
+    if ka["enableRanlux"]:
+        nskip = {0: 0, 1: 24, 2: 76, 3: 200, 4: 380}[ka["luxuaryFactor"] + 1]
+        rng = uni * ((24 + nskip) / 24.0 * 3 + 8)
+    else:
+        rng = uni * 8
+    bm = dof * 9
+    return rng + bm + 2 * POT_OPS[config]
+
+
+def roofline_for(config, ka, node_rate, clk):
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    peak = 4 * 32 * 152 * sm_mhz * 1e6 / 1e12            # Tera lane-ops/s
+    per_node = alg_ops_per_node(config, ka)
+    achieved = node_rate * per_node / 1e12
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
+            "frac": achieved / peak, "traffic": None,
+            "alg_ops_per_node": per_node,
+            "peak_basis": f"4 x 32 x 152 lanes per clock at the sampled median SM clock {sm_mhz:.0f} MHz "
+                          "(MEASURED_PEAKS.json has HBM and bf16 peaks only; this kernel uses neither)"}
+
+
+# ------------------------------------------------------------------ arms
+def run_gb300(args, rank, world):
+    from feynsimul_gb300 import build as fb
+    fb.build()
+    import torch
+    from feynsimul_gb300.kernel import PIMCKernel
+    from feynsimul_gb300.kernel_args import KernelArgs
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    setup = he3_setup if args.config == "he3" else ho_setup
+    sysm, ka, extra, workload = setup()
+    ka_obj = KernelArgs(system=sysm, seed=1000 + rank, **extra, **ka)
+    k = PIMCKernel(ka_obj)
+    paths0 = initial_paths(sysm, ka, 17 + rank)
+    k.setPaths(paths0)
+    if ka["enableRanlux"]:
+        k.initRanlux()
+        k.groupInitRanlux()
+    info = k.getInfo()
+    nodes = node_updates_per_run(ka)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        k.run()
+    # ---- device-resident throughput ----
+    clocks = ClockSampler(dev)
+    clocks.start()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()  # 512 MiB write: L2 (129 MB) holds nothing of the previous launch
+        torch.cuda.synchronize()
+        k.run()
+        times.append(k.getRunTime())
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t_dev = float(np.sum(times))
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    value = nodes * args.steps * world / t_dev
+    ms_per_step = 1e3 * t_dev / args.steps
+
+    # ---- end to end through the reference-facing API, host buffers ----
+    cudart = torch.cuda.cudart()
+    host_paths = np.ascontiguousarray(k.getPaths())
+    try:
+        cudart.cudaHostRegister(host_paths.ctypes.data, host_paths.nbytes, 0)
+        pinned = True
+    except Exception:
+        pinned = False
+    energies = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        k.setPaths(host_paths)          # H2D: this step's input paths
+        k.run()
+        ops = k.getOperators()          # D2H: per-thread operator means, reduced per walker
+        k.getPaths(out=host_paths)      # D2H: the paths the next step starts from
+        energies.append(ops[0])
+    t_e2e = time.perf_counter() - t0
+    if pinned:
+        try:
+            cudart.cudaHostUnregister(host_paths.ctypes.data)
+        except Exception:
+            pass
+    e2e_value = nodes * args.steps * world / t_e2e
+    h2d = host_paths.nbytes
+    d2h = k._nbrOfThreads * len(ka["operators"]) * 8 + host_paths.nbytes
+
+    # energy ESS/s from the per-run per-walker energy series of the e2e loop
+    series = np.array(energies)  # [steps, walkers]
+    tau = integrated_autocorr(series)
+    ess = series.shape[0] * series.shape[1] / (2.0 * tau)
+    ess_per_s = ess / (ms_per_step * 1e-3 * args.steps)
+
+    # ---- roofline: the sweep is bound by instruction issue (see roofline_for) ----
+    roof = roofline_for(args.config, ka, value / world, clk)
+
+    result = {
+        "metric": "path-node updates/s (plain Metropolis-bisection sampler)",
+        "value": value, "unit": "node-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (u32 RNG, f64 sums)",
+        "data": "synthetic, seeded",
+        "config": {"workload": workload, "sweeps_per_step": ka["operatorRuns"] * ka["metroStepsPerOperatorRun"],
+                   "node_updates_per_step": nodes, "l2": "flushed between launches (512 MiB write)",
+                   "parallelism": f"replicas x{world}", "walkers_per_block": int(info.walkers_per_block),
+                   "registers": int(info.registers), "smem_bytes": int(info.smem_bytes)},
+        "e2e": {"value": e2e_value, "unit": "node-updates/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "pinned": pinned},
+        "energy_ess_per_s": ess_per_s, "energy_tau_int_runs": tau,
+        "energy_mean": float(series[series.shape[0] // 2:].mean()),
+        "acceptance_rate": float(k.getAcceptanceRate()),
+        "gpu_launches": args.steps * 2,
+        "roofline": roof, "clocks": clk,
+    }
+    k.close()
+    return result, (sysm, ka, extra)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="he3", choices=["he3", "ho"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        setup = he3_setup if args.config == "he3" else ho_setup
+        sysm, ka, extra, workload = setup()
+        vals = []
+        for _ in range(args.warmup):
+            oracle_cpu_rate(sysm, ka, extra, seconds=1.0)
+        t_all = []
+        for _ in range(args.steps):
+            cb = oracle_cpu_rate(sysm, ka, extra, seconds=max(1.0, 60.0 / max(1, args.steps)))
+            vals.append(cb["value"])
+        v = float(np.median(vals))
+        out = {"impl": "reference", "metric": "path-node updates/s (plain Metropolis-bisection sampler)",
+               "value": v, "unit": "node-updates/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic, seeded", "config": {"workload": workload},
+               "cpu_baseline": dict(cb, value=v),
+               "e2e": {"value": v, "unit": "node-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+               "note": "the reference's OpenCL kernels need an OpenCL CPU platform, which is absent; this "
+                       "times the oracle's C restatement of the reference sweep on every host thread"}
+        print(json.dumps(out))
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    result, (sysm, ka, extra) = run_gb300(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            result["cpu_baseline"] = oracle_cpu_rate(sysm, ka, extra, seconds=args.cpu_seconds)
+        print(json.dumps(result))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1053 @@
+// fs_api.cu -- host side of libfeynsimul_gb300.so: the C ABI declared in include/feynsimul.h.
+//
+// The reference builds one OpenCL program per run configuration from a text template
+// (FeynSimul/kernel.py:215-381).  This library does the same for sm_103a: it validates the
+// configuration (kernel.py:93-211), generates CUDA source (FS_* constants + the device RNG
+// header + the plugin's userCode / potential / operators / correlators + fs_pimc.cuh),
+// compiles it with NVRTC (cached per source text, in memory and on disk), loads it with
+// cudaLibraryLoadData and owns every device buffer of the run.
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <cctype>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include "../../include/feynsimul.h"
+
+static const char *kRngSrc =
+#include "fs_rng.inc"
+    ;
+static const char *kPimcSrc =
+#include "fs_pimc.inc"
+    ;
+
+#define FS_VERSION "feynsimul_gb300 0.1 (sm_103a)"
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_thread_err;
+
+struct fs_handle {
+    fs_config cfg{};
+    int device = 0;
+    std::string source, log, err;
+    std::vector<std::string> ops, cors, hists;
+    // launch geometry
+    int tpw = 1, seg = 1, wpb = 1, block = 1, grid = 1;
+    long long n_threads = 0;
+    size_t smem = 0;
+    int regs = 0;
+    size_t ft = 4, op_elem = 8, cor_elem = 8;
+    size_t n_ops_elems = 0, n_cor_elems = 0, n_bins = 0, n_hist = 0;
+    // CUDA objects
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t k_metro = nullptr, k_rinit = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+    // device buffers
+    void *d_paths = nullptr;
+    uint32_t *d_accepts = nullptr, *d_seeds = nullptr, *d_snap = nullptr, *d_wseeds = nullptr;
+    uint32_t *d_rtab = nullptr, *d_gtab = nullptr, *d_bins = nullptr;
+    void *d_ops = nullptr, *d_cor = nullptr;
+    unsigned long long *d_hist = nullptr;
+    int *d_status = nullptr;
+    size_t g_rows = 0;
+    size_t device_bytes = 0;
+};
+
+static int fail(fs_handle *h, int code, const char *fmt, ...)
+{
+    char buf[2048];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (h)
+        h->err = buf;
+    else
+        g_thread_err = buf;
+    return code;
+}
+
+#define CUDA_TRY(h, call, code)                                                              \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail((h), (code), "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                                 \
+    } while (0)
+
+// ------------------------------------------------------------------ code generation
+// Append 'f' to unsuffixed floating literals: the reference compiles plugin code with
+// -cl-single-precision-constant (kernel.py:376-377); CUDA would otherwise promote
+// expressions such as 0.5*x to FP64.
+static std::string float_literals(const std::string &s)
+{
+    std::string out;
+    size_t i = 0, n = s.size();
+    out.reserve(n + 16);
+    auto dig = [&](size_t k) { return k < n && std::isdigit((unsigned char)s[k]); };
+    while (i < n) {
+        char c = s[i];
+        if (c == '/' && i + 1 < n && s[i + 1] == '/') {
+            size_t e = s.find('\n', i);
+            e = e == std::string::npos ? n : e;
+            out.append(s, i, e - i);
+            i = e;
+            continue;
+        }
+        if (c == '/' && i + 1 < n && s[i + 1] == '*') {
+            size_t e = s.find("*/", i + 2);
+            e = e == std::string::npos ? n : e + 2;
+            out.append(s, i, e - i);
+            i = e;
+            continue;
+        }
+        if (c == '"' || c == '\'') {
+            size_t e = i + 1;
+            while (e < n && s[e] != c) e += (s[e] == '\\') ? 2 : 1;
+            e = std::min(n, e + 1);
+            out.append(s, i, e - i);
+            i = e;
+            continue;
+        }
+        if (std::isalpha((unsigned char)c) || c == '_') {
+            size_t e = i;
+            while (e < n && (std::isalnum((unsigned char)s[e]) || s[e] == '_')) e++;
+            out.append(s, i, e - i);
+            i = e;
+            continue;
+        }
+        if (std::isdigit((unsigned char)c) || (c == '.' && dig(i + 1))) {
+            size_t j = i;
+            bool fl = false;
+            if (c == '0' && j + 1 < n && (s[j + 1] == 'x' || s[j + 1] == 'X')) {
+                j += 2;
+                while (j < n && (std::isxdigit((unsigned char)s[j]) || s[j] == '.')) {
+                    if (s[j] == '.') fl = true;
+                    j++;
+                }
+                if (j < n && (s[j] == 'p' || s[j] == 'P')) {
+                    fl = true;
+                    j++;
+                    if (j < n && (s[j] == '+' || s[j] == '-')) j++;
+                    while (dig(j)) j++;
+                }
+            } else {
+                while (dig(j)) j++;
+                if (j < n && s[j] == '.') {
+                    fl = true;
+                    j++;
+                    while (dig(j)) j++;
+                }
+                if (j < n && (s[j] == 'e' || s[j] == 'E')) {
+                    size_t k = j + 1;
+                    if (k < n && (s[k] == '+' || s[k] == '-')) k++;
+                    if (dig(k)) {
+                        fl = true;
+                        j = k;
+                        while (dig(j)) j++;
+                    }
+                }
+            }
+            size_t k = j;
+            while (k < n && (std::isalpha((unsigned char)s[k]) || s[k] == '_')) k++;
+            out.append(s, i, k - i);
+            if (fl && k == j) out += 'f';
+            i = k;
+            continue;
+        }
+        out += c;
+        i++;
+    }
+    return out;
+}
+
+static std::string fmt17(double v)
+{
+    char b[64];
+    snprintf(b, sizeof b, "%1.17e", v);  // the reference's '%1.17e' (kernel.py:298, :312)
+    return b;
+}
+
+static int nskip_for(int lux)
+{
+    switch (lux) {
+    case 0: return 0;
+    case 1: return 24;
+    case 2: return 76;
+    case 3: return 200;
+    case 4: return 380;
+    default: return lux - 24;
+    }
+}
+
+static std::string gen_prelude(bool dbl)
+{
+    std::ostringstream o;
+    o << "// generated by libfeynsimul_gb300 (" FS_VERSION ")\n";
+    o << "#define FS_DOUBLE " << (dbl ? 1 : 0) << "\n";
+    if (dbl) {
+        o << "typedef double FT;\n#define M_PI 3.14159265358979323846\n#define M_PI_2 1.57079632679489661923\n";
+    } else {
+        o << "typedef float FT;\n#define M_PI 3.14159265358979323846f\n#define M_PI_2 1.57079632679489661923f\n";
+    }
+    o << "#define FLOAT_TYPE FT\n#define FLOAT_TYPE_VECTOR FT##4\n";
+    // OpenCL built-in spellings accepted in plugin strings (physical_systems/__init__.py:5-9)
+    o << "#define native_exp exp\n#define native_log log\n#define native_sqrt sqrt\n"
+         "#define native_sin sin\n#define native_cos cos\n#define native_powr pow\n"
+         "#define native_divide(a, b) ((a) / (b))\n#define native_recip(a) ((FT)1 / (a))\n"
+         "#define half_exp exp\n#define half_log log\n#define half_sqrt sqrt\n";
+    return o.str();
+}
+
+struct GenOut {
+    std::string src;
+};
+
+static std::string gen_source(const fs_handle &h, const std::string &potential,
+                              const std::string &user_code)
+{
+    const fs_config &c = h.cfg;
+    const bool dbl = c.enable_double != 0;
+    auto lit = [&](double v) { return fmt17(v) + (dbl ? "" : "f"); };
+    auto cvt = [&](const std::string &s) { return dbl ? s : float_literals(s); };
+    std::ostringstream o;
+    o << gen_prelude(dbl);
+    const int nhist = c.hist_bins > 0 ? (int)h.hists.size() : 0;
+    const double opnorm = 1.0 / ((double)c.operator_runs * c.n_slices * c.n_walkers / (double)h.n_threads);
+    o << "#define FS_DOF " << c.dof << "\n#define FS_N " << c.n_slices << "\n#define FS_S "
+      << c.bisection_level << "\n#define FS_SEG " << h.seg << "\n#define FS_TPW " << h.tpw
+      << "\n#define FS_WPB " << h.wpb << "\n#define FS_NWALKERS " << c.n_walkers
+      << "\n#define FS_WPG " << c.walkers_per_group << "\n#define FS_NWG "
+      << (c.n_walkers / std::max(1, c.walkers_per_group)) << "\n#define FS_PARALLEL "
+      << (c.enable_parallelize_path ? 1 : 0) << "\n#define FS_RANLUX " << (c.enable_ranlux ? 1 : 0)
+      << "\n#define FS_NSKIP " << (c.enable_ranlux ? nskip_for(c.luxury_factor + 1) : 0)
+      << "\n#define FS_COMPAT " << (c.compat ? 1 : 0) << "\n#define FS_ACCUM " << c.accum
+      << "\n#define FS_FAST " << (c.fast_math ? 1 : 0) << "\n#define FS_NOPS " << h.ops.size()
+      << "\n#define FS_NCOR " << h.cors.size() << "\n#define FS_OPRUNS " << c.operator_runs
+      << "\n#define FS_MSTEPS " << c.metro_steps_per_operator_run << "\n#define FS_EPS "
+      << lit(c.beta / (double)c.n_slices) << "\n#define FS_OPNORM " << lit(opnorm)
+      << "\n#define FS_BINS " << (c.enable_bins ? 1 : 0) << "\n#define FS_NHIST " << nhist << "\n";
+    {
+        char b[64];
+        snprintf(b, sizeof b, "%.9E", (double)(c.ranlux_int_max + 1ull));
+        o << "#define FS_RIM " << b << "f\n";  // kernel.py:334: always a float literal
+    }
+    if (c.enable_bins) {
+        o << "#define FS_XMIN " << lit(c.x_min) << "\n#define FS_XMAX " << lit(c.x_max)
+          << "\n#define FS_BINRES " << c.bin_resolution_per_dof << "\n#define FS_INVBIN "
+          << lit((double)c.bin_resolution_per_dof / (c.x_max - c.x_min)) << "\n";
+    }
+    if (nhist) {
+        o << "#define FS_HLO " << lit(c.hist_lo) << "\n#define FS_HHI " << lit(c.hist_hi)
+          << "\n#define FS_HBINS " << c.hist_bins << "\n#define FS_HINVW "
+          << lit((double)c.hist_bins / (c.hist_hi - c.hist_lo)) << "\n";
+    } else {
+        o << "#define FS_HBINS 0\n";
+    }
+    o << "#define eps FS_EPS\n";  // kernel.c:31
+    o << "\n// ---- random number generators ----\n" << kRngSrc << "\n";
+    o << "\n// ---- plugin userCode ----\n" << cvt(user_code) << "\n";
+    std::ostringstream args, at;
+    for (int i = 0; i < c.dof; i++) {
+        args << (i ? ", " : "") << "FT x" << (i + 1);
+        at << (i ? ", " : "") << "(P)[" << i << " * FS_N + (i)]";
+    }
+    o << "#define FS_ARGS_AT(P, i) " << at.str() << "\n";
+    o << "__device__ __forceinline__ FT fs_pot(" << args.str() << ") { return (" << cvt(potential)
+      << "); }\n";
+    auto fn = [&](const char *name, const std::vector<std::string> &ex) {
+        if (ex.empty()) return;
+        o << "__device__ __forceinline__ void " << name << "(" << args.str() << ", FT *o) {\n";
+        for (size_t i = 0; i < ex.size(); i++) o << "    o[" << i << "] = (" << cvt(ex[i]) << ");\n";
+        o << "}\n";
+    };
+    fn("fs_ops", h.ops);
+    fn("fs_cors", h.cors);
+    if (nhist) fn("fs_hist", h.hists);
+    o << "\n// ---- sweep kernel ----\n" << kPimcSrc << "\n";
+    return o.str();
+}
+
+// ------------------------------------------------------------------ NVRTC + cache
+static std::mutex g_cache_mu;
+static std::unordered_map<std::string, std::string> g_cubins;
+
+static uint64_t fnv1a(const std::string &s, uint64_t hsh = 1469598103934665603ull)
+{
+    for (unsigned char ch : s) {
+        hsh ^= ch;
+        hsh *= 1099511628211ull;
+    }
+    return hsh;
+}
+
+static std::string cache_dir()
+{
+    const char *d = std::getenv("FS_CACHE_DIR");
+    if (d && *d) return d;
+    const char *home = std::getenv("HOME");
+    return std::string(home && *home ? home : "/tmp") + "/.cache/feynsimul_gb300";
+}
+
+static int compile_module(fs_handle *h, const std::string &src, bool fast, std::string *cubin,
+                          std::string *log)
+{
+    std::vector<std::string> opts = {"--gpu-architecture=sm_103a", "-default-device", "--std=c++17",
+                                      "-lineinfo", "--ptxas-options=-v"};
+    if (fast)
+        opts.push_back("--use_fast_math");
+    else
+        opts.push_back("--fmad=false");
+    std::string key_text = src;
+    for (auto &s : opts) key_text += "\n" + s;
+    char keybuf[64];
+    snprintf(keybuf, sizeof keybuf, "%016llx%016llx", (unsigned long long)fnv1a(key_text),
+             (unsigned long long)fnv1a(key_text, 0x9E3779B97F4A7C15ull));
+    const std::string key = keybuf;
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        auto it = g_cubins.find(key);
+        if (it != g_cubins.end()) {
+            *cubin = it->second;
+            *log = "(cached)";
+            return FS_OK;
+        }
+    }
+    const std::string path = cache_dir() + "/" + key + ".cubin";
+    {
+        std::ifstream f(path, std::ios::binary);
+        if (f) {
+            std::stringstream ss;
+            ss << f.rdbuf();
+            *cubin = ss.str();
+            if (!cubin->empty()) {
+                std::ifstream lf(path + ".log");
+                std::stringstream ls;
+                if (lf) ls << lf.rdbuf();
+                *log = "(disk cache " + path + ")\n" + ls.str();
+                std::lock_guard<std::mutex> lk(g_cache_mu);
+                g_cubins[key] = *cubin;
+                return FS_OK;
+            }
+        }
+    }
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, src.c_str(), "feynsimul_sweep.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+        return fail(h, FS_ERR_COMPILE, "nvrtcCreateProgram failed");
+    std::vector<const char *> copts;
+    for (auto &s : opts) copts.push_back(s.c_str());
+    nvrtcResult r = nvrtcCompileProgram(prog, (int)copts.size(), copts.data());
+    size_t lsz = 0;
+    nvrtcGetProgramLogSize(prog, &lsz);
+    log->assign(lsz, '\0');
+    if (lsz) nvrtcGetProgramLog(prog, &(*log)[0]);
+    if (r != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        return fail(h, FS_ERR_COMPILE, "NVRTC compilation failed: %s\n%s", nvrtcGetErrorString(r),
+                    log->substr(0, 1800).c_str());
+    }
+    size_t csz = 0;
+    nvrtcGetCUBINSize(prog, &csz);
+    cubin->assign(csz, '\0');
+    nvrtcGetCUBIN(prog, &(*cubin)[0]);
+    nvrtcDestroyProgram(&prog);
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        g_cubins[key] = *cubin;
+    }
+    // best-effort disk cache: write a temporary file, then rename it into place
+    std::string dir = cache_dir();
+    for (size_t p = 1; p <= dir.size(); p++)
+        if (p == dir.size() || dir[p] == '/') ::mkdir(dir.substr(0, p).c_str(), 0755);
+    std::string tmp = path + "." + std::to_string((long long)::getpid()) + ".tmp";
+    {
+        std::ofstream f(tmp, std::ios::binary);
+        if (f) f.write(cubin->data(), (std::streamsize)cubin->size());
+    }
+    {
+        std::ofstream lf(tmp + ".log");
+        if (lf) lf << *log;
+    }
+    std::rename((tmp + ".log").c_str(), (path + ".log").c_str());
+    std::rename(tmp.c_str(), path.c_str());
+    return FS_OK;
+}
+
+static int load_module(fs_handle *h, const std::string &cubin)
+{
+    CUDA_TRY(h, cudaLibraryLoadData(&h->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
+             FS_ERR_CUDA);
+    return FS_OK;
+}
+
+// ------------------------------------------------------------------ validation
+// The checks of kernel.py:93-211 that concern the device path; the Python layer raises the
+// reference's exception types before it gets here.
+static int validate(const fs_config &c, int nops, int ncor, int nhist)
+{
+    if (c.dof < 1 || c.dof > 256) return fail(nullptr, FS_ERR_CONFIG, "DOF must be in [1, 256]");
+    if (c.n_slices < 2 || (c.n_slices & (c.n_slices - 1)))
+        return fail(nullptr, FS_ERR_CONFIG, "Path node number, N, must be a power of 2.");
+    if (c.bisection_level < 0 || (1ll << c.bisection_level) > c.n_slices)
+        return fail(nullptr, FS_ERR_CONFIG, "2^S must be less than or equal to N.");
+    if (!(c.beta > 0.0) || !std::isfinite(c.beta)) return fail(nullptr, FS_ERR_CONFIG, "beta must be a positive float");
+    if (c.n_walkers < 1) return fail(nullptr, FS_ERR_CONFIG, "nbrOfWalkers must be >= 1");
+    if (c.walkers_per_group < 1 || c.n_walkers % c.walkers_per_group)
+        return fail(nullptr, FS_ERR_CONFIG,
+                    "The number of walkers must be a multiple of the number of walkers per work group.");
+    if (c.operator_runs < 1 || c.metro_steps_per_operator_run < 0)
+        return fail(nullptr, FS_ERR_CONFIG, "operatorRuns must be >= 1 and metroStepsPerOperatorRun >= 0");
+    if (c.enable_parallelize_path && (c.n_slices >> c.bisection_level) > 1024)
+        return fail(nullptr, FS_ERR_CONFIG, "N / 2^S threads per walker must not exceed 1024");
+    if (c.enable_ranlux) {
+        int lux = c.luxury_factor + 1;
+        int ns = nskip_for(lux);
+        if (c.luxury_factor < 0 || (lux > 4 && lux < 24) || ns % 4 != 0 || (ns != 0 && ns < 24))
+            return fail(nullptr, FS_ERR_CONFIG, "luxuaryFactor needs to be an uint >= 0 (0-3, or >= 23 with p-24 a multiple of 4).");
+        if (c.ranlux_int_max < 1 || c.ranlux_int_max > 0xFFFFFFFFull)
+            return fail(nullptr, FS_ERR_CONFIG, "ranluxIntMax needs to be an uint > 0.");
+    }
+    if (c.enable_bins) {
+        if (c.bin_resolution_per_dof < 1 || !(c.x_max > c.x_min))
+            return fail(nullptr, FS_ERR_CONFIG, "xMin < xMax and binResolutionPerDOF >= 1 are needed when enableBins is True.");
+        double nb = std::pow((double)c.bin_resolution_per_dof, c.dof);
+        if (nb > 1e9) return fail(nullptr, FS_ERR_CONFIG, "binResolutionPerDOF ** DOF bins is too large");
+    }
+    if (nhist > 0 && (c.hist_bins < 1 || c.hist_bins > 16384 || !(c.hist_hi > c.hist_lo)))
+        return fail(nullptr, FS_ERR_CONFIG, "histogram needs 1..16384 bins and hist_lo < hist_hi");
+    if (c.accum < 0 || c.accum > 3) return fail(nullptr, FS_ERR_CONFIG, "accum must be 0..3");
+    if (nops < 0 || ncor < 0 || nops > 64 || ncor > 16)
+        return fail(nullptr, FS_ERR_CONFIG, "at most 64 operators and 16 correlators");
+    if (c.walkers_per_block < 0) return fail(nullptr, FS_ERR_CONFIG, "walkers_per_block must be >= 0");
+    return FS_OK;
+}
+
+static void free_buffers(fs_handle *h)
+{
+    void *bufs[] = {h->d_paths, h->d_accepts, h->d_seeds, h->d_snap, h->d_wseeds, h->d_rtab,
+                    h->d_gtab, h->d_bins, h->d_ops, h->d_cor, h->d_hist, h->d_status};
+    for (void *p : bufs)
+        if (p) cudaFree(p);
+}
+
+static int dalloc(fs_handle *h, void **p, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(h, FS_ERR_OOM, "Unable to allocate global memory on device, out of memory? (%zu bytes: %s)",
+                    bytes, cudaGetErrorString(e));
+    }
+    CUDA_TRY(h, cudaMemsetAsync(*p, 0, bytes, h->stream), FS_ERR_CUDA);
+    h->device_bytes += bytes;
+    return FS_OK;
+}
+
+// Host-only half of fs_create: validation, geometry, source generation, NVRTC compile.
+static int prepare(const fs_config *cfg, const char *potential, const char *user_code,
+                   const char *const *operators, int32_t n_operators, const char *const *correlators,
+                   int32_t n_correlators, const char *const *histograms, int32_t n_histograms,
+                   fs_handle **out, std::string *cubin_out)
+{
+    if (!cfg || !potential || !out) return fail(nullptr, FS_ERR_CONFIG, "null argument");
+    *out = nullptr;
+    int rc = validate(*cfg, n_operators, n_correlators, n_histograms);
+    if (rc) return rc;
+    fs_handle *h = new fs_handle();
+    h->cfg = *cfg;
+    const fs_config &c = h->cfg;
+    for (int i = 0; i < n_operators; i++) h->ops.push_back(operators[i] ? operators[i] : "0");
+    for (int i = 0; i < n_correlators; i++) h->cors.push_back(correlators[i] ? correlators[i] : "1");
+    if (c.hist_bins > 0)
+        for (int i = 0; i < n_histograms; i++) h->hists.push_back(histograms[i] ? histograms[i] : "0");
+
+    // ---- geometry (kernel.py:192-211) ----
+    h->seg = 1 << c.bisection_level;
+    h->tpw = c.enable_parallelize_path ? (c.n_slices >> c.bisection_level) : 1;
+    h->n_threads = (long long)c.n_walkers * h->tpw;
+    h->ft = c.enable_double ? 8 : 4;
+    const size_t per_walker = (size_t)(c.dof + (int)h->cors.size()) * c.n_slices * h->ft;
+    const size_t hist_bytes = (size_t)(c.hist_bins > 0 && !h->hists.empty() ? c.hist_bins : 0) * 4;
+    if (c.walkers_per_block > 0) {
+        h->wpb = c.walkers_per_block;
+    } else if (h->tpw > 32) {
+        h->wpb = 1;
+    } else {
+        int target = h->tpw == 1 ? 64 : 128;
+        h->wpb = std::max(1, target / h->tpw);
+        while (h->wpb > 1 && per_walker * h->wpb + hist_bytes > 100 * 1024) h->wpb /= 2;
+    }
+    h->wpb = std::min(h->wpb, c.n_walkers);
+    if (h->tpw > 32 && h->wpb != 1) {
+        delete h;
+        return fail(nullptr, FS_ERR_CONFIG, "walkers_per_block must be 1 when N / 2^S > 32");
+    }
+    if (h->tpw <= 32 && 32 % h->tpw != 0) {
+        delete h;
+        return fail(nullptr, FS_ERR_CONFIG, "internal: threads per walker must divide 32");
+    }
+    h->block = h->wpb * h->tpw;
+    if (h->block > 1024) {
+        delete h;
+        return fail(nullptr, FS_ERR_CONFIG, "walkers_per_block * threads per walker exceeds 1024");
+    }
+    h->grid = (c.n_walkers + h->wpb - 1) / h->wpb;
+    h->smem = per_walker * h->wpb + hist_bytes;
+    if (h->smem > 227 * 1024) {
+        delete h;
+        return fail(nullptr, FS_ERR_CONFIG,
+                    "a walker's path does not fit in shared memory (%zu bytes per CTA); lower walkers_per_block",
+                    h->smem);
+    }
+
+    // ---- source + compile ----
+    h->source = gen_source(*h, potential, user_code ? user_code : "");
+    rc = compile_module(h, h->source, c.fast_math != 0, cubin_out, &h->log);
+    if (rc) {
+        g_thread_err = h->err;
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return FS_OK;
+}
+
+extern "C" int fs_compile_only(const fs_config *cfg, const char *potential, const char *user_code,
+                               const char *const *operators, int32_t n_operators,
+                               const char *const *correlators, int32_t n_correlators,
+                               const char *const *histograms, int32_t n_histograms, char *log,
+                               size_t log_capacity)
+{
+    fs_handle *h = nullptr;
+    std::string cubin;
+    int rc = prepare(cfg, potential, user_code, operators, n_operators, correlators, n_correlators,
+                     histograms, n_histograms, &h, &cubin);
+    std::string text = rc ? g_thread_err : h->log;
+    if (log && log_capacity) {
+        size_t k = std::min(log_capacity - 1, text.size());
+        memcpy(log, text.data(), k);
+        log[k] = 0;
+    }
+    delete h;
+    return rc;
+}
+
+extern "C" int fs_create(const fs_config *cfg, const char *potential, const char *user_code,
+                         const char *const *operators, int32_t n_operators,
+                         const char *const *correlators, int32_t n_correlators,
+                         const char *const *histograms, int32_t n_histograms, fs_handle **out)
+{
+    fs_handle *h = nullptr;
+    std::string cubin;
+    int rc = prepare(cfg, potential, user_code, operators, n_operators, correlators, n_correlators,
+                     histograms, n_histograms, &h, &cubin);
+    if (rc) return rc;
+    const fs_config &c = h->cfg;
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) {
+        fail(nullptr, FS_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+        delete h;
+        return FS_ERR_CUDA;
+    }
+#define CREATE_TRY(call)                                      \
+    do {                                                      \
+        int r_ = (call);                                      \
+        if (r_) {                                             \
+            g_thread_err = h->err;                            \
+            free_buffers(h);                                  \
+            if (h->lib) cudaLibraryUnload(h->lib);            \
+            if (h->stream) cudaStreamDestroy(h->stream);      \
+            delete h;                                         \
+            return r_;                                        \
+        }                                                     \
+    } while (0)
+    auto cu = [&](cudaError_t err, const char *what) -> int {
+        if (err != cudaSuccess) return fail(h, FS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
+        return FS_OK;
+    };
+    CREATE_TRY(cu(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate"));
+    CREATE_TRY(cu(cudaEventCreate(&h->ev0), "cudaEventCreate"));
+    CREATE_TRY(cu(cudaEventCreate(&h->ev1), "cudaEventCreate"));
+    CREATE_TRY(load_module(h, cubin));
+    CREATE_TRY(cu(cudaLibraryGetKernel(&h->k_metro, h->lib, "fs_metropolis"), "fs_metropolis"));
+    CREATE_TRY(cu(cudaLibraryGetKernel(&h->k_rinit, h->lib, "fs_ranlux_init"), "fs_ranlux_init"));
+    CREATE_TRY(cu(cudaFuncSetAttribute((const void *)h->k_metro, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)h->smem), "cudaFuncSetAttribute"));
+    {
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, (const void *)h->k_metro) == cudaSuccess) h->regs = fa.numRegs;
+        else cudaGetLastError();
+    }
+
+    // ---- buffers (kernel.py:386-457) ----
+    const size_t W = c.n_walkers, T = h->n_threads, N = c.n_slices;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) cudaGetLastError();
+    h->op_elem = c.accum == 0 ? h->ft : (c.accum == 2 ? 4 : 8);
+    h->n_ops_elems = T * h->ops.size() * (c.accum == 3 ? 3 : 1);
+    h->cor_elem = c.accum == 0 ? h->ft : 8;
+    h->n_cor_elems = W * h->cors.size() * (N / 2);
+    h->n_bins = c.enable_bins ? (size_t)std::llround(std::pow((double)c.bin_resolution_per_dof, c.dof)) : 0;
+    h->n_hist = h->hists.empty() ? 0 : (size_t)c.hist_bins;
+    h->g_rows = c.compat ? T : W;
+    size_t need = W * c.dof * N * h->ft + T * 4 + h->n_ops_elems * h->op_elem + h->n_cor_elems * h->cor_elem +
+                  h->n_bins * 4 + h->n_hist * 8 +
+                  (c.enable_ranlux ? (T + h->g_rows) * 112 : ((T + 1) * 16 * 2 + W * 16));
+    if (free_b && need > free_b) {
+        fail(nullptr, FS_ERR_OOM,
+             "Unable to allocate global memory on device, out of memory? (need %zu bytes, %zu free)", need, free_b);
+        cudaStreamDestroy(h->stream);
+        cudaLibraryUnload(h->lib);
+        delete h;
+        return FS_ERR_OOM;
+    }
+    CREATE_TRY(dalloc(h, &h->d_paths, W * c.dof * N * h->ft));
+    CREATE_TRY(dalloc(h, (void **)&h->d_accepts, T * 4));
+    if (c.enable_ranlux) {
+        CREATE_TRY(dalloc(h, (void **)&h->d_rtab, T * 112));
+        CREATE_TRY(dalloc(h, (void **)&h->d_gtab, h->g_rows * 112));
+    } else {
+        CREATE_TRY(dalloc(h, (void **)&h->d_seeds, (T + 1) * 16));
+        if (c.compat) CREATE_TRY(dalloc(h, (void **)&h->d_snap, (T + 1) * 16));
+        CREATE_TRY(dalloc(h, (void **)&h->d_wseeds, W * 16));
+    }
+    CREATE_TRY(dalloc(h, &h->d_ops, h->n_ops_elems * h->op_elem));
+    CREATE_TRY(dalloc(h, &h->d_cor, h->n_cor_elems * h->cor_elem));
+    CREATE_TRY(dalloc(h, (void **)&h->d_bins, h->n_bins * 4));
+    CREATE_TRY(dalloc(h, (void **)&h->d_hist, h->n_hist * 8));
+    CREATE_TRY(dalloc(h, (void **)&h->d_status, 16));
+    CREATE_TRY(cu(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"));
+#undef CREATE_TRY
+    *out = h;
+    return FS_OK;
+}
+
+extern "C" int fs_destroy(fs_handle *h)
+{
+    if (!h) return FS_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_buffers(h);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->lib) cudaLibraryUnload(h->lib);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return FS_OK;
+}
+
+extern "C" const char *fs_last_error(const fs_handle *h) { return h ? h->err.c_str() : g_thread_err.c_str(); }
+extern "C" const char *fs_build_log(const fs_handle *h) { return h ? h->log.c_str() : ""; }
+extern "C" const char *fs_source(const fs_handle *h) { return h ? h->source.c_str() : ""; }
+extern "C" const char *fs_version(void) { return FS_VERSION; }
+
+extern "C" int fs_query(const fs_handle *h, fs_info *info)
+{
+    if (!h || !info) return FS_ERR_CONFIG;
+    info->n_threads = h->n_threads;
+    info->threads_per_walker = h->tpw;
+    info->walkers_per_block = h->wpb;
+    info->block_threads = h->block;
+    info->grid_blocks = h->grid;
+    info->smem_bytes = (int64_t)h->smem;
+    info->registers = h->regs;
+    info->device_bytes = (int64_t)h->device_bytes;
+    info->nodes_per_move = h->seg - 1;
+    info->uniforms_per_move = 2ll * h->cfg.dof * (h->seg - 1) + 1;
+    return FS_OK;
+}
+
+// ------------------------------------------------------------------ host <-> device
+static int copy_in(fs_handle *h, void *dst, const void *src, size_t bytes, size_t expect)
+{
+    if (!h) return FS_ERR_CONFIG;
+    if (bytes != expect) return fail(h, FS_ERR_IO, "buffer has %zu bytes, expected %zu", bytes, expect);
+    if (!dst) return fail(h, FS_ERR_STATE, "buffer not used by this configuration");
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
+    return FS_OK;
+}
+
+static int copy_out(fs_handle *h, void *dst, const void *src, size_t bytes, size_t expect)
+{
+    if (!h) return FS_ERR_CONFIG;
+    if (bytes != expect) return fail(h, FS_ERR_IO, "buffer has %zu bytes, expected %zu", bytes, expect);
+    if (!src) return fail(h, FS_ERR_STATE, "buffer not used by this configuration");
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
+    return FS_OK;
+}
+
+static size_t path_elems(const fs_handle *h) { return (size_t)h->cfg.n_walkers * h->cfg.dof * h->cfg.n_slices; }
+
+extern "C" int fs_set_paths(fs_handle *h, const void *host, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_in(h, h->d_paths, host, n * h->ft, path_elems(h) * h->ft);
+}
+extern "C" int fs_get_paths(fs_handle *h, void *host, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_out(h, host, h->d_paths, n * h->ft, path_elems(h) * h->ft);
+}
+extern "C" int fs_set_xorshift_seeds(fs_handle *h, const uint32_t *rows, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_in(h, h->d_seeds, rows, n * 16, (h->n_threads + 1) * 16);
+}
+extern "C" int fs_get_xorshift_seeds(fs_handle *h, uint32_t *rows, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_out(h, rows, h->d_seeds, n * 16, (h->n_threads + 1) * 16);
+}
+extern "C" int fs_set_walker_seeds(fs_handle *h, const uint32_t *rows, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_in(h, h->d_wseeds, rows, n * 16, (size_t)h->cfg.n_walkers * 16);
+}
+extern "C" int fs_get_walker_seeds(fs_handle *h, uint32_t *rows, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_out(h, rows, h->d_wseeds, n * 16, (size_t)h->cfg.n_walkers * 16);
+}
+
+static int ranlux_seed_rows(fs_handle *h, uint32_t *tab, size_t rows, const uint64_t *xs, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    if (!tab) return fail(h, FS_ERR_STATE, "RANLUX is not enabled for this handle");
+    if (n != rows) return fail(h, FS_ERR_IO, "got %zu seed values, expected %zu", n, rows);
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    void *d_xs = nullptr;
+    CUDA_TRY(h, cudaMallocAsync(&d_xs, n * 8, h->stream), FS_ERR_OOM);
+    CUDA_TRY(h, cudaMemcpyAsync(d_xs, xs, n * 8, cudaMemcpyHostToDevice, h->stream), FS_ERR_CUDA);
+    int ni = (int)n;
+    void *args[] = {&tab, &d_xs, &ni};
+    CUDA_TRY(h, cudaLaunchKernel((const void *)h->k_rinit, dim3((unsigned)((n + 127) / 128)), dim3(128), args, 0,
+                                 h->stream), FS_ERR_LAUNCH);
+    CUDA_TRY(h, cudaFreeAsync(d_xs, h->stream), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
+    return FS_OK;
+}
+
+extern "C" int fs_ranlux_init(fs_handle *h, const uint64_t *xs, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return ranlux_seed_rows(h, h->d_rtab, (size_t)h->n_threads, xs, n);
+}
+extern "C" int fs_ranlux_group_init(fs_handle *h, const uint64_t *xs, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return ranlux_seed_rows(h, h->d_gtab, h->g_rows, xs, n);
+}
+extern "C" int fs_get_ranlux_tables(fs_handle *h, uint32_t *tab, size_t nt, uint32_t *gtab, size_t ng)
+{
+    if (!h) return FS_ERR_CONFIG;
+    int rc = FS_OK;
+    if (tab) rc = copy_out(h, tab, h->d_rtab, nt * 112, (size_t)h->n_threads * 112);
+    if (!rc && gtab) rc = copy_out(h, gtab, h->d_gtab, ng * 112, h->g_rows * 112);
+    return rc;
+}
+extern "C" int fs_set_ranlux_tables(fs_handle *h, const uint32_t *tab, size_t nt, const uint32_t *gtab, size_t ng)
+{
+    if (!h) return FS_ERR_CONFIG;
+    int rc = FS_OK;
+    if (tab) rc = copy_in(h, h->d_rtab, tab, nt * 112, (size_t)h->n_threads * 112);
+    if (!rc && gtab) rc = copy_in(h, h->d_gtab, gtab, ng * 112, h->g_rows * 112);
+    return rc;
+}
+
+// ------------------------------------------------------------------ run
+struct FsArgsHost {  // mirrors FsArgs in fs_pimc.cuh
+    void *paths;
+    uint32_t *accepts, *seeds;
+    const uint32_t *seed_snap;
+    uint32_t *walker_seeds, *rtab, *gtab;
+    void *op_means, *cor_means;
+    uint32_t *bins;
+    unsigned long long *hist;
+    int *status;
+    double opnorm;
+};
+
+extern "C" int fs_run(fs_handle *h, int32_t n_launches)
+{
+    if (!h) return FS_ERR_CONFIG;
+    if (n_launches < 1) return fail(h, FS_ERR_CONFIG, "n_launches must be >= 1");
+    const fs_config &c = h->cfg;
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    FsArgsHost a;
+    a.paths = h->d_paths;
+    a.accepts = h->d_accepts;
+    a.seeds = h->d_seeds;
+    a.seed_snap = h->d_snap;
+    a.walker_seeds = h->d_wseeds;
+    a.rtab = h->d_rtab;
+    a.gtab = h->d_gtab;
+    a.op_means = h->d_ops;
+    a.cor_means = h->d_cor;
+    a.bins = h->d_bins;
+    a.hist = h->d_hist;
+    a.status = h->d_status;
+    a.opnorm = 1.0 / ((double)c.operator_runs * c.n_slices * c.n_walkers / (double)h->n_threads);
+    void *args[] = {&a};
+    CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), FS_ERR_CUDA);
+    for (int i = 0; i < n_launches; i++) {
+        if (h->d_snap)
+            CUDA_TRY(h, cudaMemcpyAsync(h->d_snap, h->d_seeds, (h->n_threads + 1) * 16, cudaMemcpyDeviceToDevice,
+                                        h->stream), FS_ERR_CUDA);
+        CUDA_TRY(h, cudaLaunchKernel((const void *)h->k_metro, dim3(h->grid), dim3(h->block), args, h->smem, h->stream),
+                 FS_ERR_LAUNCH);
+    }
+    CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), FS_ERR_CUDA);
+    h->timed = true;
+    return FS_OK;
+}
+
+extern "C" int fs_sync(fs_handle *h)
+{
+    if (!h) return FS_ERR_CONFIG;
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
+    return FS_OK;
+}
+
+// host watchdog: poll the stream instead of blocking forever (kernel.py:499-506 analogue)
+extern "C" int fs_sync_timeout(fs_handle *h, double seconds)
+{
+    if (!h) return FS_ERR_CONFIG;
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(h->stream);
+        if (e == cudaSuccess) return FS_OK;
+        if (e != cudaErrorNotReady) return fail(h, FS_ERR_LAUNCH, "stream error: %s", cudaGetErrorString(e));
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el > seconds)
+            return fail(h, FS_ERR_TIMEOUT, "work still running after %.3f s (limit %.3f s)", el, seconds);
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+}
+
+extern "C" int fs_get_run_time(fs_handle *h, double *seconds)
+{
+    if (!h || !seconds) return FS_ERR_CONFIG;
+    if (!h->timed) return fail(h, FS_ERR_STATE, "no run yet");
+    CUDA_TRY(h, cudaEventSynchronize(h->ev1), FS_ERR_LAUNCH);
+    float ms = 0.f;
+    CUDA_TRY(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1), FS_ERR_CUDA);
+    *seconds = ms * 1e-3;
+    return FS_OK;
+}
+
+template <class T>
+static void widen(const std::vector<unsigned char> &raw, double *out, size_t n)
+{
+    const T *p = (const T *)raw.data();
+    for (size_t i = 0; i < n; i++) out[i] = (double)p[i];
+}
+
+extern "C" int fs_get_operators(fs_handle *h, double *out, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    if (n != h->n_ops_elems) return fail(h, FS_ERR_IO, "expected %zu operator values", h->n_ops_elems);
+    std::vector<unsigned char> raw(n * h->op_elem + 1);
+    int rc = copy_out(h, raw.data(), h->d_ops, n * h->op_elem, n * h->op_elem);
+    if (rc) return rc;
+    if (h->op_elem == 4) widen<float>(raw, out, n);
+    else widen<double>(raw, out, n);
+    return FS_OK;
+}
+
+extern "C" int fs_get_correlator(fs_handle *h, double *out, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    if (n != h->n_cor_elems) return fail(h, FS_ERR_IO, "expected %zu correlator values", h->n_cor_elems);
+    std::vector<unsigned char> raw(n * h->cor_elem + 1);
+    int rc = copy_out(h, raw.data(), h->d_cor, n * h->cor_elem, n * h->cor_elem);
+    if (rc) return rc;
+    if (h->cor_elem == 4) widen<float>(raw, out, n);
+    else widen<double>(raw, out, n);
+    return FS_OK;
+}
+
+extern "C" int fs_get_accepts(fs_handle *h, uint32_t *out, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_out(h, out, h->d_accepts, n * 4, (size_t)h->n_threads * 4);
+}
+extern "C" int fs_get_bins(fs_handle *h, uint32_t *out, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_out(h, out, h->d_bins, n * 4, h->n_bins * 4);
+}
+extern "C" int fs_get_histogram(fs_handle *h, uint64_t *out, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_out(h, out, h->d_hist, n * 8, h->n_hist * 8);
+}
+extern "C" int fs_zero_accumulators(fs_handle *h)
+{
+    if (!h) return FS_ERR_CONFIG;
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    if (h->n_cor_elems) CUDA_TRY(h, cudaMemsetAsync(h->d_cor, 0, h->n_cor_elems * h->cor_elem, h->stream), FS_ERR_CUDA);
+    if (h->n_bins) CUDA_TRY(h, cudaMemsetAsync(h->d_bins, 0, h->n_bins * 4, h->stream), FS_ERR_CUDA);
+    if (h->n_hist) CUDA_TRY(h, cudaMemsetAsync(h->d_hist, 0, h->n_hist * 8, h->stream), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
+    return FS_OK;
+}
+
+// ------------------------------------------------------------------ RNG stream modules
+static std::mutex g_rng_mu;
+static std::unordered_map<int, cudaLibrary_t> g_rng_libs;  // per (device, lux)
+
+static int rng_module(int lux, cudaLibrary_t *lib)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(nullptr, FS_ERR_CUDA, "no CUDA device");
+    const int key = dev * 4096 + lux;
+    std::lock_guard<std::mutex> lk(g_rng_mu);
+    auto it = g_rng_libs.find(key);
+    if (it != g_rng_libs.end()) {
+        *lib = it->second;
+        return FS_OK;
+    }
+    std::ostringstream o;
+    o << gen_prelude(false) << "#define FS_NSKIP " << nskip_for(lux) << "\n#define FS_RNG_ONLY 1\n"
+      << "#define FS_N 2\n#define FS_S 0\n#define FS_SEG 1\n#define FS_TPW 1\n#define FS_WPB 1\n"
+         "#define FS_NWALKERS 1\n#define FS_WPG 1\n#define FS_NWG 1\n#define FS_PARALLEL 0\n"
+         "#define FS_RANLUX 0\n#define FS_COMPAT 0\n#define FS_ACCUM 1\n#define FS_FAST 0\n"
+         "#define FS_NOPS 0\n#define FS_NCOR 0\n#define FS_OPRUNS 1\n#define FS_MSTEPS 1\n"
+         "#define FS_EPS 1.0f\n#define FS_OPNORM 1.0f\n#define FS_BINS 0\n#define FS_NHIST 0\n"
+         "#define FS_HBINS 0\n#define FS_RIM 4.294967296E+09f\n#define FS_DOF 1\n"
+      << kRngSrc << "\n#define FS_ARGS_AT(P, i) (P)[(i)]\n"
+      << "__device__ FT fs_pot(FT x1) { return x1; }\n" << kPimcSrc;
+    fs_handle tmp;
+    std::string cubin, log;
+    int rc = compile_module(&tmp, o.str(), false, &cubin, &log);
+    if (rc) return fail(nullptr, rc, "%s", tmp.err.c_str());
+    cudaError_t e = cudaLibraryLoadData(lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) return fail(nullptr, FS_ERR_CUDA, "cudaLibraryLoadData: %s", cudaGetErrorString(e));
+    g_rng_libs[key] = *lib;
+    return FS_OK;
+}
+
+#define G_TRY(call)                                                                     \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            fail(nullptr, FS_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));         \
+            goto done;                                                                  \
+        }                                                                               \
+    } while (0)
+
+extern "C" int fs_rng_ranlux_stream(int32_t lux, const uint64_t *xs, int32_t n, int32_t calls, float *out,
+                                    uint32_t *states)
+{
+    int ns = nskip_for(lux);
+    if (lux < 0 || (lux > 4 && lux < 24) || ns % 4 || (ns && ns < 24) || n < 1 || calls < 0)
+        return fail(nullptr, FS_ERR_CONFIG, "bad RANLUX stream request");
+    cudaLibrary_t lib;
+    int rc = rng_module(lux, &lib);
+    if (rc) return rc;
+    cudaKernel_t k;
+    void *dx = nullptr, *dout = nullptr, *dst = nullptr;
+    rc = FS_ERR_CUDA;
+    G_TRY(cudaLibraryGetKernel(&k, lib, "fs_ranlux_dump"));
+    G_TRY(cudaMalloc(&dx, (size_t)n * 8));
+    G_TRY(cudaMalloc(&dout, (size_t)n * calls * 16 + 16));
+    G_TRY(cudaMalloc(&dst, (size_t)n * 112));
+    G_TRY(cudaMemcpy(dx, xs, (size_t)n * 8, cudaMemcpyHostToDevice));
+    {
+        void *args[] = {&dx, &n, &calls, &dout, &dst};
+        G_TRY(cudaLaunchKernel((const void *)k, dim3((n + 63) / 64), dim3(64), args, 0, 0));
+    }
+    G_TRY(cudaDeviceSynchronize());
+    G_TRY(cudaMemcpy(out, dout, (size_t)n * calls * 16, cudaMemcpyDeviceToHost));
+    if (states) G_TRY(cudaMemcpy(states, dst, (size_t)n * 112, cudaMemcpyDeviceToHost));
+    rc = FS_OK;
+done:
+    if (dx) cudaFree(dx);
+    if (dout) cudaFree(dout);
+    if (dst) cudaFree(dst);
+    return rc;
+}
+
+extern "C" int fs_rng_ranlux_stream64(int32_t lux, const uint64_t *xs, int32_t n, int32_t calls, double *out)
+{
+    int ns = nskip_for(lux);
+    if (lux < 0 || (lux > 4 && lux < 24) || ns % 4 || (ns && ns < 24) || n < 1 || calls < 0)
+        return fail(nullptr, FS_ERR_CONFIG, "bad RANLUX stream request");
+    cudaLibrary_t lib;
+    int rc = rng_module(lux, &lib);
+    if (rc) return rc;
+    cudaKernel_t k;
+    void *dx = nullptr, *dout = nullptr;
+    rc = FS_ERR_CUDA;
+    G_TRY(cudaLibraryGetKernel(&k, lib, "fs_ranlux_dump64"));
+    G_TRY(cudaMalloc(&dx, (size_t)n * 8));
+    G_TRY(cudaMalloc(&dout, (size_t)n * calls * 32 + 32));
+    G_TRY(cudaMemcpy(dx, xs, (size_t)n * 8, cudaMemcpyHostToDevice));
+    {
+        void *args[] = {&dx, &n, &calls, &dout};
+        G_TRY(cudaLaunchKernel((const void *)k, dim3((n + 63) / 64), dim3(64), args, 0, 0));
+    }
+    G_TRY(cudaDeviceSynchronize());
+    G_TRY(cudaMemcpy(out, dout, (size_t)n * calls * 32, cudaMemcpyDeviceToHost));
+    rc = FS_OK;
+done:
+    if (dx) cudaFree(dx);
+    if (dout) cudaFree(dout);
+    return rc;
+}
+
+extern "C" int fs_rng_xorshift_stream(uint32_t *states, int32_t n, int32_t draws, uint32_t *out, float *fout)
+{
+    if (n < 1 || draws < 0) return fail(nullptr, FS_ERR_CONFIG, "bad xorshift stream request");
+    cudaLibrary_t lib;
+    int rc = rng_module(0, &lib);
+    if (rc) return rc;
+    cudaKernel_t k;
+    void *ds = nullptr, *dout = nullptr, *dfo = nullptr;
+    rc = FS_ERR_CUDA;
+    G_TRY(cudaLibraryGetKernel(&k, lib, "fs_xorshift_dump"));
+    G_TRY(cudaMalloc(&ds, (size_t)n * 16));
+    G_TRY(cudaMalloc(&dout, (size_t)n * draws * 4 + 4));
+    G_TRY(cudaMalloc(&dfo, (size_t)n * draws * 4 + 4));
+    G_TRY(cudaMemcpy(ds, states, (size_t)n * 16, cudaMemcpyHostToDevice));
+    {
+        void *args[] = {&ds, &n, &draws, &dout, &dfo};
+        G_TRY(cudaLaunchKernel((const void *)k, dim3((n + 63) / 64), dim3(64), args, 0, 0));
+    }
+    G_TRY(cudaDeviceSynchronize());
+    G_TRY(cudaMemcpy(out, dout, (size_t)n * draws * 4, cudaMemcpyDeviceToHost));
+    G_TRY(cudaMemcpy(fout, dfo, (size_t)n * draws * 4, cudaMemcpyDeviceToHost));
+    G_TRY(cudaMemcpy(states, ds, (size_t)n * 16, cudaMemcpyDeviceToHost));
+    rc = FS_OK;
+done:
+    if (ds) cudaFree(ds);
+    if (dout) cudaFree(dout);
+    if (dfo) cudaFree(dfo);
+    return rc;
+}

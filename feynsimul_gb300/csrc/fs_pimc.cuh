@@ -1,0 +1,568 @@
+// fs_pimc.cuh -- the Metropolis-bisection path-integral sweep (sm_103a, NVRTC-specialised).
+//
+// fs_api.cu builds one module per run configuration, exactly as the reference rebuilds
+// its OpenCL program per configuration (FeynSimul/kernel.py:215-381): the FS_* macros,
+// the RNG header and the plugin's userCode / potential / operator / correlator strings are
+// pasted in front of this file.
+//
+// Work decomposition (kernel.py:192-211 semantics, GB300 layout):
+//   * one CUDA thread per reference work-item: a walker's N/2^S "segment threads" bisect
+//     their own 2^S-slice segment of the walker's path at a per-step random offset shared
+//     by the walker (kernel.c:709-721); walker mode is one thread per walker;
+//   * FS_WPB walkers per CTA; a walker's threads sit in one warp (TPW <= 32, synchronised
+//     by __syncwarp on the walker's lanes) or fill the CTA (TPW > 32, __syncthreads);
+//   * the walker's whole path [DOF][N] lives in shared memory for the whole launch,
+//     loaded and stored once with coalesced (float4 where aligned) copies of the
+//     reference's walker-major layout;
+//   * RNG state in registers; global accepts / seeds / operator means keep the
+//     reference's thread-id layout (kernel.c:541) so the host reductions are unchanged;
+//   * operator and correlator running sums in registers (FP64 unless the
+//     reference-order FP32 mode is selected), histogram counts privatised per CTA in
+//     shared memory.
+#pragma once
+
+#define FS_HALF_N (FS_N / 2)
+#define FS_THREADS (FS_NWALKERS * FS_TPW)
+#define FS_BLOCK (FS_WPB * FS_TPW)
+#define FS_LPT ((FS_HALF_N + FS_TPW - 1) / FS_TPW)  // correlator lags owned per thread
+#define FS_COR_REGS (FS_LPT * FS_NCOR <= 16)
+
+#if FS_DOUBLE
+#define FS_ADD __dadd_rn
+#define FS_SUB __dsub_rn
+#define FS_MUL __dmul_rn
+#define FS_DIV __ddiv_rn
+#define FS_SQRT_RN __dsqrt_rn
+#define FS_LOG log
+#define FS_SQRT sqrt
+#define FS_SIN sin
+#define FS_EXP exp
+#define FS_TWO_PI 6.283185307179586
+#else
+#define FS_ADD __fadd_rn
+#define FS_SUB __fsub_rn
+#define FS_MUL __fmul_rn
+#define FS_DIV __fdiv_rn
+#define FS_SQRT_RN __fsqrt_rn
+#if FS_FAST
+#define FS_LOG __logf
+#define FS_SIN __sinf
+#define FS_EXP __expf
+#else
+#define FS_LOG logf
+#define FS_SIN sinf
+#define FS_EXP expf
+#endif
+#define FS_SQRT sqrtf
+#define FS_TWO_PI 6.28318548f  // 2 * float(pi), as the reference's single-precision constant
+#endif
+
+// ---------------------------------------------------------------- streams
+#if FS_RANLUX
+#if FS_DOUBLE
+typedef FsRanluxStream64<FS_NSKIP> FsUStream;
+#else
+typedef FsRanluxStream<FS_NSKIP> FsUStream;
+#endif
+__device__ __forceinline__ FT fs_uniform(FsUStream &g) { return g.next(); }
+typedef FsUStream FsIStream;
+#else
+typedef FsXorshift FsUStream;
+typedef FsXorshift FsIStream;
+__device__ __forceinline__ FT fs_uniform(FsXorshift &g)
+{
+#if FS_DOUBLE
+    return fs_xs_double(g);
+#else
+    return fs_xs_float(g);
+#endif
+}
+#endif
+
+// offset of the walker's segment grid for one Metropolis step (kernel.c:715, :718)
+__device__ __forceinline__ fs_u32 fs_offset(FsIStream &g, fs_u32 range)
+{
+#if FS_RANLUX
+    FT f = g.next();
+#if FS_COMPAT
+    // (uint)(f * (ranluxIntMax+1)) (kernel.c:206): low 8 bits are zero
+    return ((fs_u32)FS_MUL(f, (FT)FS_RIM)) & (range - 1u);
+#else
+    return ((fs_u32)FS_MUL(f, (FT)range)) & (range - 1u);
+#endif
+#else
+    return fs_xs_next(g) & (range - 1u);
+#endif
+}
+
+#if FS_SEG > 1
+#define FS_OLD_N ((FS_SEG - 1) * FS_DOF)
+#else
+#define FS_OLD_N 1
+#endif
+
+#if FS_RANLUX
+#define FS_MOVE_UNROLL _Pragma("unroll 1")
+#else
+#define FS_MOVE_UNROLL _Pragma("unroll")
+#endif
+
+// kernel.c:258-399 on a shared-memory path P[DOF][N]
+__device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, const FT *sigma)
+{
+    FT old[FS_OLD_N];
+    FT aOld = (FT)0;
+#pragma unroll
+    for (int i = 1; i < FS_SEG; i++) {
+        const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
+#pragma unroll
+        for (int d = 0; d < FS_DOF; d++) old[(i - 1) * FS_DOF + d] = P[d * FS_N + p];
+    }
+    FS_MOVE_UNROLL
+    for (int i = 1; i < FS_SEG; i++) {
+        const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
+        aOld = FS_ADD(aOld, FS_MUL((FT)FS_EPS, fs_pot(FS_ARGS_AT(P, p))));
+    }
+    FS_MOVE_UNROLL
+    for (int n = 1; n <= FS_S; n++) {
+        const int half = 1 << (FS_S - n);
+        const FT sig = sigma[n];
+        FS_MOVE_UNROLL
+        for (int i = 0; i < (1 << (n - 1)); i++) {
+            const fs_u32 m = ((fs_u32)((1 + 2 * i) * half) + start) & (FS_N - 1);
+            const fs_u32 l = ((fs_u32)(i * 2 * half) + start) & (FS_N - 1);
+            const fs_u32 r = ((fs_u32)((i + 1) * 2 * half) + start) & (FS_N - 1);
+            FS_MOVE_UNROLL
+            for (int d = 0; d < FS_DOF; d++) {
+                const FT u = fs_uniform(g);
+                const FT v = fs_uniform(g);
+                FT rz = (FT)0;
+                if (v != (FT)0) {
+                    // sigma_n * sqrt(-2 log v) * sin(2 pi u), left to right (kernel.c:352-353)
+                    rz = FS_MUL(FS_MUL(sig, FS_SQRT(FS_MUL((FT)-2, FS_LOG(v)))),
+                                FS_SIN(FS_MUL((FT)FS_TWO_PI, u)));
+                }
+                P[d * FS_N + m] = FS_ADD(FS_MUL((FT)0.5, FS_ADD(P[d * FS_N + l], P[d * FS_N + r])), rz);
+            }
+        }
+    }
+    FT aNew = (FT)0;
+    FS_MOVE_UNROLL
+    for (int i = 1; i < FS_SEG; i++) {
+        const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
+        aNew = FS_ADD(aNew, FS_MUL((FT)FS_EPS, fs_pot(FS_ARGS_AT(P, p))));
+    }
+    const FT acc = fs_uniform(g);
+    if (FS_EXP(FS_SUB(aOld, aNew)) < acc) {
+#pragma unroll
+        for (int i = 1; i < FS_SEG; i++) {
+            const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
+#pragma unroll
+            for (int d = 0; d < FS_DOF; d++) P[d * FS_N + p] = old[(i - 1) * FS_DOF + d];
+        }
+        return 0;
+    }
+    return 1;
+}
+
+struct FsArgs {
+    FT *paths;                 // [walkers][DOF][N]
+    fs_u32 *accepts;           // [threads]
+    fs_u32 *seeds;             // xorshift [threads+1][4]
+    const fs_u32 *seed_snap;   // xorshift, reference-compatible mode: table at launch start
+    fs_u32 *walker_seeds;      // xorshift, fixed mode: [walkers][4]
+    fs_u32 *rtab;              // RANLUX [threads][28]
+    fs_u32 *gtab;              // RANLUX compat [threads][28], fixed [walkers][28]
+    void *op_means;            // [threads][nOps] (study mode: [threads][nOps][3] double)
+    void *cor_means;           // [walkers][nCorr][N/2]
+    fs_u32 *bins;              // [res^DOF]
+    fs_u64 *hist;              // [hist bins]
+    int *status;
+    double opnorm;
+};
+
+__device__ __forceinline__ int fs_thread_id(int w, int t)
+{
+#if FS_PARALLEL
+    const int g = w / FS_WPG, l1 = w % FS_WPG;
+    return g * FS_TPW + t + l1 * FS_NWG * FS_TPW;  // kernel.c:539-541
+#else
+    return w;
+#endif
+}
+
+#if FS_ACCUM == 0
+typedef FT FsCorAcc;
+#else
+typedef double FsCorAcc;
+#endif
+
+__device__ __forceinline__ void fs_kahan(float &s, float &c, float x)
+{
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+}
+
+#ifndef FS_RNG_ONLY
+extern "C" __global__ void __launch_bounds__(FS_BLOCK) fs_metropolis(FsArgs a)
+{
+    extern __shared__ __align__(16) unsigned char fs_smem[];
+    FT *s_path = (FT *)fs_smem;                                  // [WPB][DOF*N]
+    FT *s_cor = s_path + FS_WPB * FS_DOF * FS_N;                 // [WPB][NCOR][N]
+    fs_u32 *s_hist = (fs_u32 *)(s_cor + FS_WPB * FS_NCOR * FS_N);  // [HBINS]
+
+    const int tid_b = threadIdx.x;
+    const int wl = tid_b / FS_TPW;
+    const int t = tid_b % FS_TPW;
+    const int w0 = blockIdx.x * FS_WPB;
+    const int w = w0 + wl;
+    const int n_here = min(FS_WPB, FS_NWALKERS - w0);
+    const bool active = wl < n_here;
+
+    // ---- path in (coalesced) ----
+    {
+        const size_t base = (size_t)w0 * FS_DOF * FS_N;
+        const int count = n_here * FS_DOF * FS_N;
+#if !FS_DOUBLE
+        if ((FS_DOF * FS_N) % 4 == 0) {
+            const float4 *src = (const float4 *)(a.paths + base);
+            float4 *dst = (float4 *)s_path;
+            for (int i = tid_b; i < count / 4; i += FS_BLOCK) dst[i] = src[i];
+        } else
+#endif
+        {
+            for (int i = tid_b; i < count; i += FS_BLOCK) s_path[i] = a.paths[base + i];
+        }
+#if FS_NHIST > 0
+        for (int i = tid_b; i < FS_HBINS; i += FS_BLOCK) s_hist[i] = 0u;
+#endif
+    }
+    __syncthreads();
+
+    if (active) {
+#if FS_TPW <= 32
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned wmask = FS_TPW == 32 ? 0xFFFFFFFFu
+                                            : (((1u << FS_TPW) - 1u) << (lane / FS_TPW * FS_TPW));
+#define FS_WSYNC() __syncwarp(wmask)
+#else
+#define FS_WSYNC() __syncthreads()
+#endif
+        FT *P = s_path + wl * FS_DOF * FS_N;
+        const int tid = fs_thread_id(w, t);
+
+        // sigma table (kernel.c:608-618)
+        FT sigma[FS_S + 1];
+        sigma[0] = FS_MUL((FT)FS_SEG, (FT)FS_EPS);
+        {
+            int twoPow = 1;
+#pragma unroll
+            for (int i = 1; i <= FS_S; i++) {
+                twoPow *= 2;
+                sigma[i] = FS_SQRT_RN(FS_DIV(FS_MUL((FT)FS_SEG, (FT)FS_EPS), FS_MUL((FT)2, (FT)twoPow)));
+            }
+        }
+
+        // ---- RNG state ----
+        FsUStream fs;
+        FsIStream is;
+#if FS_RANLUX
+        fs_rl_load(fs.st, a.rtab + (size_t)tid * 28);
+        fs.count = 0u;
+#if FS_COMPAT
+        fs_rl_load(is.st, a.gtab + (size_t)tid * 28);
+#else
+        fs_rl_load(is.st, a.gtab + (size_t)w * 28);
+#endif
+        is.count = 0u;
+#else
+        {
+            const uint4 s4 = *(const uint4 *)(a.seeds + (size_t)tid * 4);
+            fs.x = s4.x; fs.y = s4.y; fs.z = s4.z; fs.w = s4.w;
+#if FS_COMPAT
+#if FS_PARALLEL
+            const int row = (w / FS_WPG) + (w % FS_WPG) * FS_NWG;  // kernel.c:568
+#else
+            const int row = w;  // local size 1
+#endif
+            const uint4 g4 = *(const uint4 *)(a.seed_snap + (size_t)row * 4);
+#else
+            const uint4 g4 = *(const uint4 *)(a.walker_seeds + (size_t)w * 4);
+#endif
+            is.x = g4.x; is.y = g4.y; is.z = g4.z; is.w = g4.w;
+        }
+#endif
+        fs_u32 n_acc = 0u;
+
+#if FS_NOPS > 0
+        FT opr[FS_NOPS];
+        double opd[FS_NOPS];
+        float opf[FS_NOPS], opks[FS_NOPS], opkc[FS_NOPS];
+#pragma unroll
+        for (int i = 0; i < FS_NOPS; i++) {
+            opr[i] = (FT)0; opd[i] = 0.0; opf[i] = 0.0f; opks[i] = 0.0f; opkc[i] = 0.0f;
+        }
+#endif
+#if FS_NCOR > 0
+        FsCorAcc *g_cor = (FsCorAcc *)a.cor_means + (size_t)w * FS_NCOR * FS_HALF_N;
+        FT *C = s_cor + wl * FS_NCOR * FS_N;
+#if FS_COR_REGS
+        FsCorAcc cacc[FS_NCOR][FS_LPT];
+#pragma unroll
+        for (int c = 0; c < FS_NCOR; c++)
+#pragma unroll
+            for (int j = 0; j < FS_LPT; j++) {
+                const int tau = t + j * FS_TPW;
+                cacc[c][j] = tau < FS_HALF_N ? g_cor[c * FS_HALF_N + tau] : (FsCorAcc)0;
+            }
+#endif
+#endif
+
+        // ---- sweeps (kernel.c:628-799) ----
+#pragma unroll 1
+        for (int run = 0; run < FS_OPRUNS; run++) {
+#pragma unroll 1
+            for (int step = 0; step < FS_MSTEPS; step++) {
+#if FS_PARALLEL
+                const fs_u32 off = fs_offset(is, FS_SEG);
+                const fs_u32 start = (off + (fs_u32)(FS_SEG * t)) & (FS_N - 1);
+#else
+                const fs_u32 start = fs_offset(is, FS_N);
+#endif
+                n_acc += (fs_u32)fs_bisect(P, start, fs, sigma);
+                FS_WSYNC();
+            }
+            // ---- measurement (kernel.c:734-797) ----
+#if FS_PARALLEL
+            const int s_lo = t * FS_SEG, s_hi = (t + 1) * FS_SEG;
+#else
+            const int s_lo = 0, s_hi = FS_N;
+#endif
+#pragma unroll 1
+            for (int s = s_lo; s < s_hi; s++) {
+#if FS_NOPS > 0
+                FT ov[FS_NOPS];
+                fs_ops(FS_ARGS_AT(P, s), ov);
+#pragma unroll
+                for (int i = 0; i < FS_NOPS; i++) {
+#if FS_ACCUM == 0
+                    opr[i] = FS_ADD(opr[i], ov[i]);
+#elif FS_ACCUM == 1
+                    opd[i] = __dadd_rn(opd[i], (double)ov[i]);
+#elif FS_ACCUM == 2
+                    fs_kahan(opks[i], opkc[i], (float)ov[i]);
+#else
+                    opf[i] = __fadd_rn(opf[i], (float)ov[i]);
+                    fs_kahan(opks[i], opkc[i], (float)ov[i]);
+                    opd[i] = __dadd_rn(opd[i], (double)ov[i]);
+#endif
+                }
+#endif
+#if FS_BINS
+                {
+                    int ok = 1, inc = 1, bi = 0;
+#pragma unroll
+                    for (int d = 0; d < FS_DOF; d++) {
+                        const FT x = P[d * FS_N + s];
+                        if (x < (FT)FS_XMIN || x >= (FT)FS_XMAX) ok = 0;
+                        bi += (int)((fs_u32)FS_MUL(FS_SUB(x, (FT)FS_XMIN), (FT)FS_INVBIN)) * inc;
+                        inc *= FS_BINRES;
+                    }
+                    if (ok) atomicAdd(a.bins + bi, 1u);
+                }
+#endif
+#if FS_NHIST > 0
+                {
+                    FT hv[FS_NHIST];
+                    fs_hist(FS_ARGS_AT(P, s), hv);
+#pragma unroll
+                    for (int h = 0; h < FS_NHIST; h++) {
+                        const FT x = hv[h];
+                        if (x >= (FT)FS_HLO && x < (FT)FS_HHI) {
+                            const int b = (int)FS_MUL(FS_SUB(x, (FT)FS_HLO), (FT)FS_HINVW);
+                            if (b >= 0 && b < FS_HBINS) atomicAdd(s_hist + b, 1u);
+                        }
+                    }
+                }
+#endif
+#if FS_NCOR > 0
+                {
+                    FT cv[FS_NCOR];
+                    fs_cors(FS_ARGS_AT(P, s), cv);
+#pragma unroll
+                    for (int c = 0; c < FS_NCOR; c++) C[c * FS_N + s] = cv[c];
+                }
+#endif
+            }
+#if FS_NCOR > 0
+            FS_WSYNC();
+            // lags tau = t + j*TPW owned by this thread
+#pragma unroll
+            for (int c = 0; c < FS_NCOR; c++) {
+                const FT *Cc = C + c * FS_N;
+#if FS_COR_REGS
+#pragma unroll
+#else
+#pragma unroll 1
+#endif
+                for (int j = 0; j < FS_LPT; j++) {
+                    const int tau = t + j * FS_TPW;
+                    if (tau >= FS_HALF_N) continue;
+#if FS_COR_REGS
+                    FsCorAcc acc = cacc[c][j];
+#else
+                    FsCorAcc acc = g_cor[c * FS_HALF_N + tau];
+#endif
+#if FS_ACCUM == 0 && FS_PARALLEL
+                    // the reference's summation order (kernel.c:736-793)
+#pragma unroll 1
+                    for (int k = 0; k < FS_SEG; k++)
+#pragma unroll 1
+                        for (int cti = 0; cti < FS_HALF_N; cti++) {
+                            const int tp = (tau - cti + FS_HALF_N) % FS_HALF_N;
+                            if (tp >= FS_TPW) continue;
+                            const int s1 = tp * FS_SEG + k;
+                            acc = FS_ADD(acc, FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]));
+                        }
+#else
+#pragma unroll 4
+                    for (int s1 = 0; s1 < FS_N; s1++) {
+#if FS_ACCUM == 0
+                        acc = FS_ADD(acc, FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]));
+#else
+                        acc = __dadd_rn(acc, (double)FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]));
+#endif
+                    }
+#endif
+#if FS_COR_REGS
+                    cacc[c][j] = acc;
+#else
+                    g_cor[c * FS_HALF_N + tau] = acc;
+#endif
+                }
+            }
+#endif
+            FS_WSYNC();
+        }
+
+        // ---- epilogue (kernel.c:801-836) ----
+        a.accepts[tid] = n_acc;
+#if FS_NOPS > 0
+#pragma unroll
+        for (int i = 0; i < FS_NOPS; i++) {
+            const size_t o = (size_t)tid * FS_NOPS + i;
+#if FS_ACCUM == 0
+            ((FT *)a.op_means)[o] = FS_MUL(opr[i], (FT)FS_OPNORM);
+#elif FS_ACCUM == 1
+            ((double *)a.op_means)[o] = __dmul_rn(opd[i], a.opnorm);
+#elif FS_ACCUM == 2
+            ((float *)a.op_means)[o] = __fmul_rn(opks[i], (float)FS_OPNORM);
+#else
+            ((double *)a.op_means)[3 * o + 0] = (double)__fmul_rn(opf[i], (float)FS_OPNORM);
+            ((double *)a.op_means)[3 * o + 1] = (double)__fmul_rn(opks[i], (float)FS_OPNORM);
+            ((double *)a.op_means)[3 * o + 2] = __dmul_rn(opd[i], a.opnorm);
+#endif
+        }
+#endif
+#if FS_NCOR > 0 && FS_COR_REGS
+#pragma unroll
+        for (int c = 0; c < FS_NCOR; c++)
+#pragma unroll
+            for (int j = 0; j < FS_LPT; j++) {
+                const int tau = t + j * FS_TPW;
+                if (tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = cacc[c][j];
+            }
+#endif
+#if FS_RANLUX
+        fs_rl_store(fs.st, a.rtab + (size_t)tid * 28);
+#if FS_COMPAT
+        fs_rl_store(is.st, a.gtab + (size_t)tid * 28);
+#else
+        if (t == 0) fs_rl_store(is.st, a.gtab + (size_t)w * 28);
+#endif
+#else
+        *(uint4 *)(a.seeds + (size_t)tid * 4) = make_uint4(fs.x, fs.y, fs.z, fs.w);
+#if !FS_COMPAT
+        if (t == 0) *(uint4 *)(a.walker_seeds + (size_t)w * 4) = make_uint4(is.x, is.y, is.z, is.w);
+#endif
+#endif
+#undef FS_WSYNC
+    }
+    __syncthreads();
+
+    // ---- path out (coalesced) ----
+    {
+        const size_t base = (size_t)w0 * FS_DOF * FS_N;
+        const int count = n_here * FS_DOF * FS_N;
+#if !FS_DOUBLE
+        if ((FS_DOF * FS_N) % 4 == 0) {
+            float4 *dst = (float4 *)(a.paths + base);
+            const float4 *src = (const float4 *)s_path;
+            for (int i = tid_b; i < count / 4; i += FS_BLOCK) dst[i] = src[i];
+        } else
+#endif
+        {
+            for (int i = tid_b; i < count; i += FS_BLOCK) a.paths[base + i] = s_path[i];
+        }
+#if FS_NHIST > 0
+        for (int i = tid_b; i < FS_HBINS; i += FS_BLOCK)
+            if (s_hist[i]) atomicAdd(a.hist + i, (fs_u64)s_hist[i]);
+#endif
+    }
+}
+#endif  // FS_RNG_ONLY
+
+// RANLUX state-table seeding: row i from the 64-bit value xs[i] (ranluxcl_init)
+extern "C" __global__ void fs_ranlux_init(fs_u32 *tab, const fs_u64 *xs, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    FsRanlux r;
+    fs_rl_seed(r, xs[i]);
+    fs_rl_store(r, tab + (size_t)i * 28);
+}
+
+// stream dumps used by the RNG parity tests
+extern "C" __global__ void fs_ranlux_dump(const fs_u64 *xs, int n, int n_calls, float *out, fs_u32 *states)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    FsRanlux r;
+    fs_rl_seed(r, xs[i]);
+#pragma unroll 1
+    for (int c = 0; c < n_calls; c++) {
+        float o0, o1, o2, o3;
+        fs_rl_next4<FS_NSKIP>(r, o0, o1, o2, o3);
+        float *o = out + ((size_t)i * n_calls + c) * 4;
+        o[0] = o0; o[1] = o1; o[2] = o2; o[3] = o3;
+    }
+    fs_rl_store(r, states + (size_t)i * 28);
+}
+
+extern "C" __global__ void fs_ranlux_dump64(const fs_u64 *xs, int n, int n_calls, double *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    FsRanluxStream64<FS_NSKIP> g;
+    fs_rl_seed(g.st, xs[i]);
+    g.count = 0u;
+#pragma unroll 1
+    for (int c = 0; c < 4 * n_calls; c++) out[(size_t)i * 4 * n_calls + c] = g.next();
+}
+
+extern "C" __global__ void fs_xorshift_dump(fs_u32 *states, int n, int n_draws, fs_u32 *out, float *fout)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    FsXorshift s;
+    s.x = states[4 * i]; s.y = states[4 * i + 1]; s.z = states[4 * i + 2]; s.w = states[4 * i + 3];
+#pragma unroll 1
+    for (int k = 0; k < n_draws; k++) {
+        FsXorshift c = s;
+        fout[(size_t)i * n_draws + k] = fs_xs_float(c);
+        out[(size_t)i * n_draws + k] = fs_xs_next(s);
+    }
+    states[4 * i] = s.x; states[4 * i + 1] = s.y; states[4 * i + 2] = s.z; states[4 * i + 3] = s.w;
+}

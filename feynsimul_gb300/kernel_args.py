@@ -1,0 +1,99 @@
+"""KernelArgs: the run-parameter bag of the reference (FeynSimul/kernel_args.py:21-217).
+
+Same constructor signature and attribute names, so reference scripts work unchanged.
+Keyword-only additions of this engine:
+
+* ``compat`` (False): reference-compatible random-number use -- per-thread xorshift rows
+  with the walker's integer stream aliased to a seed row and never written back
+  (kernel.c:568-572), RANLUX tables all seeded from ``seeds[0]`` (kernel.c:155) and
+  RANLUX integers whose low bits are zero (kernel.c:206).  The default fixes these.
+* ``accumulation`` ("fp64"): operator / correlator running sums: "fp64", "fp32" (the
+  reference's FP32 sums in its order), "kahan" (compensated FP32) or "study" (all three
+  side by side, for the precision study).
+* ``fastMath`` (True): fast transcendental intrinsics, as the reference's
+  ``-cl-fast-relaxed-math`` build; False gives IEEE functions and no FMA contraction.
+* ``histograms`` / ``histRange`` / ``histBins``: plugin expressions binned into one shared
+  histogram (e.g. the pair distances of a cluster).
+* ``walkersPerBlock`` (0 = automatic): walkers per CUDA thread block.
+* ``seed`` (None): master seed for the seed tables; None draws from ``np.random`` exactly
+  as kernel.py:412-426 does.
+"""
+
+
+class KernelArgs:
+
+    def __init__(self,
+                 system,
+                 nbrOfWalkers,
+                 N,
+                 beta,
+                 enableOperator,
+                 enableCorrelator,
+                 enableBisection,
+                 enablePathShift,
+                 enableSingleNodeMove,
+                 enableBins,
+                 nbrOfWalkersPerWorkGroup,
+                 enableDouble=None,
+                 enableRanlux=None,
+                 luxuaryFactor=None,
+                 ranluxIntMax=None,
+                 S=None,
+                 alpha=None,
+                 PSAlpha=None,
+                 enableParallelizePath=None,
+                 metroStepsPerOperatorRun=None,
+                 enableGlobalPath=None,
+                 enableGlobalOldPath=None,
+                 operators=None,
+                 operatorRuns=None,
+                 correlators=None,
+                 xMin=None,
+                 xMax=None,
+                 binResolutionPerDOF=None,
+                 *,
+                 compat=False,
+                 accumulation="fp64",
+                 fastMath=True,
+                 histograms=None,
+                 histRange=None,
+                 histBins=None,
+                 walkersPerBlock=0,
+                 seed=None):
+        self.system = system
+        self.nbrOfWalkers = nbrOfWalkers
+        self.N = N
+        self.S = S
+        self.beta = beta
+        self.nbrOfWalkersPerWorkGroup = nbrOfWalkersPerWorkGroup
+        self.enablePathShift = enablePathShift
+        self.enableDouble = enableDouble
+        self.enableSingleNodeMove = enableSingleNodeMove
+        self.alpha = alpha
+        self.PSAlpha = PSAlpha
+        self.enableOperator = enableOperator
+        self.enableRanlux = enableRanlux
+        self.luxuaryFactor = luxuaryFactor
+        self.ranluxIntMax = ranluxIntMax
+        self.operatorRuns = operatorRuns
+        self.operators = operators
+        self.metroStepsPerOperatorRun = metroStepsPerOperatorRun
+        self.enableCorrelator = enableCorrelator
+        self.correlators = correlators
+        self.enableBins = enableBins
+        self.xMin = xMin
+        self.xMax = xMax
+        self.binResolutionPerDOF = binResolutionPerDOF
+        self.enableBisection = enableBisection
+        self.enableParallelizePath = enableParallelizePath
+        self.enableGlobalPath = enableGlobalPath
+        self.enableGlobalOldPath = enableGlobalOldPath
+        # additions
+        self.compat = compat
+        self.accumulation = accumulation
+        self.fastMath = fastMath
+        self.histograms = histograms
+        self.histRange = histRange
+        self.histBins = histBins
+        self.walkersPerBlock = walkersPerBlock
+        self.seed = seed

@@ -1,0 +1,258 @@
+"""Helium-4 clusters with the LM2M2 pair potential, as plugin objects.
+
+Counterpart of the reference's FeynSimul/physical_systems/lm2m2_cluster.py:6-95 (which
+builds the same system with sympy, Python 2) and lm2m2.h:17-147 (the pair potential).
+This module writes the C code itself:
+
+* pair potential: Aziz & Slaman (1991) LM2M2, in Kelvin for r in Angstrom,
+  V(r) = eps [A exp(-alpha x + beta x^2) - F(x) (c6/x^6 + c8/x^8 + c10/x^10) + Va(x)],
+  x = r / r_m, F(x) = exp(-(D/x - 1)^2) for x < D (else 1), add-on
+  Va(x) = A_a (sin(2 pi (x - x1)/(x2 - x1) - pi/2) + 1) on x1 <= x <= x2;
+* coordinates: mass-scaled Jacobi vectors of n equal masses (lm2m2_cluster.py:69 and
+  jacobi.py:3-36): xi_0 = (r_0 - r_1) sqrt(m/2),
+  xi_k = (mean(r_0..r_k) - r_{k+1}) sqrt((k+1) m / (k+2)); the centre of mass drops
+  out, leaving DOF = 3 (n - 1), so the kinetic term is |d xi / d tau|^2 / 2;
+* units (lm2m2_cluster.py:21-28): length Angstrom, energy Kelvin, beta = 1 / T, and
+  m = M_He * (1 Angstrom)^2 k_B / hbar^2;
+* operators: the virial energy V + (1/2) sum_k x_k dV/dx_k (lm2m2_cluster.py:75-76), which
+  for pair potentials of r^2 is sum_pairs [V + r^2 dV/d(r^2)]; the sum of squared pair
+  distances (:79-82); and the pair distances themselves for the pair-distance histogram.
+
+The reference's derivative routine adds 1.0 inside the add-on term
+(lm2m2.h:143, ``Aa*(cos(...)*B+1.0)``), which is not the derivative of Va; its energy
+estimator is therefore biased for pairs with x1 <= x <= x2.  ``referenceDerivative=True``
+reproduces that form for comparisons; the default uses the correct derivative.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+HE_MASS = 6.64647617e-27  # kg (lm2m2_cluster.py:21)
+HBAR = 1.05457148e-34      # J s
+KB = 1.3806503e-23         # J / K
+
+# LM2M2 parameters (Aziz & Slaman 1991)
+EPS_K = 10.97
+RM = 2.9695
+A_STAR = 1.89635353e5
+ALPHA = 10.70203539
+BETA_STAR = -1.90740649
+C6, C8, C10 = 1.34687065, 0.41308398, 0.17060159
+D_CUT = 1.4088
+A_ADD = 0.0026
+X1_ADD, X2_ADD = 1.003535949, 1.454790369
+
+# Ground-state energies quoted by the reference for n = 3..10 (lm2m2_cluster.py:17-19),
+# magnitudes in K.
+GROUND_STATES = [0.0872, 0.387, 0.901, 1.605, 2.478, 3.489, 4.641, 5.904]
+
+
+def lm2m2_c_code(reference_derivative: bool = False) -> str:
+    """C source of lm2m2_r2(r^2) [K] and dlm2m2_dr2(r^2) = dV/d(r^2) [K / Angstrom^2]."""
+    add_term = "(cs * B + 1.0)" if reference_derivative else "(cs * B)"
+    return f"""
+inline FLOAT_TYPE fs_sq(FLOAT_TYPE v) {{ return v * v; }}
+inline FLOAT_TYPE lm2m2_r2(FLOAT_TYPE r2)
+{{
+    FLOAT_TYPE x = sqrt(r2) * {1.0 / RM!r};
+    FLOAT_TYPE ix2 = 1.0 / (x * x);
+    FLOAT_TYPE rat = ((({C10!r} * ix2 + {C8!r}) * ix2) + {C6!r}) * ix2 * ix2 * ix2;
+    if (x < {D_CUT!r}) {{
+        if (x > {0.0005 / RM!r}) {{
+            FLOAT_TYPE q = {D_CUT!r} / x - 1.0;
+            rat = rat * exp(-q * q);
+        }} else {{
+            rat = 0.0;
+        }}
+    }}
+    FLOAT_TYPE v = {A_STAR!r} * exp(x * ({BETA_STAR!r} * x - {ALPHA!r})) - rat;
+    if (x >= {X1_ADD!r} && x <= {X2_ADD!r}) {{
+        FLOAT_TYPE B = {2.0 * np.pi / (X2_ADD - X1_ADD)!r};
+        v = v + {A_ADD!r} * (sin(B * (x - {X1_ADD!r}) - M_PI_2) + 1.0);
+    }}
+    return {EPS_K!r} * v;
+}}
+inline FLOAT_TYPE dlm2m2_dr2(FLOAT_TYPE r2)
+{{
+    FLOAT_TYPE r = sqrt(r2);
+    FLOAT_TYPE x = r * {1.0 / RM!r};
+    FLOAT_TYPE ix = 1.0 / x;
+    FLOAT_TYPE ix2 = ix * ix;
+    FLOAT_TYPE ix6 = ix2 * ix2 * ix2;
+    FLOAT_TYPE rat = (({C10!r} * ix2 + {C8!r}) * ix2 + {C6!r}) * ix6;
+    FLOAT_TYPE drat = -((({10.0 * C10!r} * ix2 + {8.0 * C8!r}) * ix2 + {6.0 * C6!r}) * ix6 * ix);
+    FLOAT_TYPE dfr;
+    if (x < {D_CUT!r}) {{
+        if (x > {0.0005 / RM!r}) {{
+            FLOAT_TYPE q = {D_CUT!r} * ix - 1.0;
+            FLOAT_TYPE F = exp(-q * q);
+            dfr = F * drat + F * (2.0 * q * {D_CUT!r} * ix2) * rat;
+        }} else {{
+            dfr = 0.0;
+        }}
+    }} else {{
+        dfr = drat;
+    }}
+    FLOAT_TYPE dv = {A_STAR!r} * exp(x * ({BETA_STAR!r} * x - {ALPHA!r})) * ({2.0 * BETA_STAR!r} * x - {ALPHA!r}) - dfr;
+    if (x >= {X1_ADD!r} && x <= {X2_ADD!r}) {{
+        FLOAT_TYPE B = {2.0 * np.pi / (X2_ADD - X1_ADD)!r};
+        FLOAT_TYPE cs = cos(B * (x - {X1_ADD!r}) - M_PI_2);
+        dv = dv + {A_ADD!r} * {add_term};
+    }}
+    return {EPS_K!r} * dv / ({2.0 * RM!r} * r);
+}}
+"""
+
+
+def lm2m2_numpy(r, reference_derivative=False):
+    """FP64 numpy evaluation of V(r) [K] and dV/d(r^2), for tests and analysis."""
+    r = np.asarray(r, dtype=np.float64)
+    x = r / RM
+    rat = C6 / x ** 6 + C8 / x ** 8 + C10 / x ** 10
+    drat = -6 * C6 / x ** 7 - 8 * C8 / x ** 9 - 10 * C10 / x ** 11
+    q = D_CUT / x - 1.0
+    F = np.where(x < D_CUT, np.exp(-q * q), 1.0)
+    dF = np.where(x < D_CUT, F * 2.0 * q * D_CUT / x ** 2, 0.0)
+    tiny = x <= 0.0005 / RM
+    frat = np.where(tiny & (x < D_CUT), 0.0, F * rat)
+    dfrat = np.where(tiny & (x < D_CUT), 0.0, F * drat + dF * rat)
+    base = A_STAR * np.exp(-ALPHA * x + BETA_STAR * x * x)
+    vb = base - frat
+    dvb = base * (-ALPHA + 2 * BETA_STAR * x) - dfrat
+    B = 2 * np.pi / (X2_ADD - X1_ADD)
+    win = (x >= X1_ADD) & (x <= X2_ADD)
+    va = np.where(win, A_ADD * (np.sin(B * (x - X1_ADD) - np.pi / 2) + 1.0), 0.0)
+    cs = np.cos(B * (x - X1_ADD) - np.pi / 2)
+    dva = np.where(win, A_ADD * (cs * B + (1.0 if reference_derivative else 0.0)), 0.0)
+    v = EPS_K * (vb + va)
+    dv_dr2 = EPS_K * (dvb + dva) / (RM * 2.0 * r)
+    return v, dv_dr2
+
+
+def jacobi_matrix(n: int, m: float) -> np.ndarray:
+    """J with xi = J r for n equal masses; rows 0..n-2 relative, row n-1 the scaled centre."""
+    J = np.zeros((n, n))
+    J[0, 0], J[0, 1] = np.sqrt(m / 2.0), -np.sqrt(m / 2.0)
+    for k in range(1, n - 1):
+        s = np.sqrt((k + 1) * m / (k + 2))
+        J[k, :k + 1] = s / (k + 1)
+        J[k, k + 1] = -s
+    J[n - 1, :] = np.sqrt(n * m) / n
+    return J
+
+
+class Lm2m2Cluster:
+    """n helium-4 atoms at temperature T [K] with the LM2M2 pair potential."""
+
+    def __init__(self, n: int, T: float, referenceDerivative: bool = False):
+        if n < 2:
+            raise Exception("n must be >=2")
+        d = 3
+        self.n = n
+        self.T = float(T)
+        self.DOF = (n - 1) * d
+        self.rUnit = 1e-10
+        self.potentialUnit = KB
+        self.beta = self.potentialUnit / (KB * self.T)
+        self.m = HE_MASS * self.rUnit ** 2 / HBAR ** 2 * self.potentialUnit
+        if 3 <= n <= 10:
+            self.groundStateEnergy = -GROUND_STATES[n - 3]
+        J = jacobi_matrix(n, self.m)
+        self.J = J
+        Jinv = np.linalg.inv(J)
+        self.B = Jinv[:, : n - 1]  # position (relative to the centre) from the relative xi
+        self.pairs = [(a, b) for a in range(n) for b in range(a + 1, n)]
+        xs = [f"x{i + 1}" for i in range(self.DOF)]
+        args = ", ".join(f"FLOAT_TYPE {v}" for v in xs)
+
+        def comp(coefs, dim):
+            terms = [f"{float(c)!r} * {xs[3 * k + dim]}" for k, c in enumerate(coefs) if abs(c) > 1e-15]
+            return " + ".join(terms) if terms else "0.0"
+
+        # positions relative to the centre of mass, then pair sums
+        pos = []
+        for a in range(n):
+            for dim in range(3):
+                pos.append(f"    FLOAT_TYPE p{a}_{dim} = {comp(self.B[a], dim)};")
+        r2 = {}
+        for (a, b) in self.pairs:
+            r2[(a, b)] = " + ".join(f"fs_sq(p{a}_{dim} - p{b}_{dim})" for dim in range(3))
+        body_pos = "\n".join(pos)
+        pot_sum = " + ".join(f"lm2m2_r2({r2[p]})" for p in self.pairs)
+        vir_terms = []
+        for i, p in enumerate(self.pairs):
+            vir_terms.append(f"    {{ FLOAT_TYPE q = {r2[p]}; e += lm2m2_r2(q) + q * dlm2m2_dr2(q); }}")
+        msr = " + ".join(r2[p] for p in self.pairs)
+        self.userCode = lm2m2_c_code(referenceDerivative) + f"""
+inline FLOAT_TYPE lm2m2_cluster_potential({args})
+{{
+{body_pos}
+    return {pot_sum};
+}}
+inline FLOAT_TYPE lm2m2_cluster_virial_energy({args})
+{{
+{body_pos}
+    FLOAT_TYPE e = 0.0;
+{chr(10).join(vir_terms)}
+    return e;
+}}
+inline FLOAT_TYPE lm2m2_cluster_pair_r2_sum({args})
+{{
+{body_pos}
+    return {msr};
+}}
+"""
+        call = ", ".join(xs)
+        self.potential = f"lm2m2_cluster_potential({call})"
+        self.energyOp = f"lm2m2_cluster_virial_energy({call})"
+        self.meanSquaredRadiusOp = f"lm2m2_cluster_pair_r2_sum({call})"
+        # pair distances [Angstrom], one expression per pair (histogram input)
+        self.pairDistanceOps = tuple(
+            "sqrt(" + " + ".join(
+                f"fs_sq({comp(self.B[a] - self.B[b], dim)})" for dim in range(3)) + ")"
+            for (a, b) in self.pairs)
+
+    # ---- coordinates -------------------------------------------------------------
+    def positions_to_jacobi(self, r):
+        """r [..., n, 3] (Angstrom) -> relative Jacobi coordinates [..., DOF]."""
+        r = np.asarray(r, dtype=np.float64)
+        xi = np.einsum("ij,...jd->...id", self.J, r)[..., : self.n - 1, :]
+        return xi.reshape(*r.shape[:-2], self.DOF)
+
+    def jacobi_to_positions(self, x):
+        """[..., DOF] -> positions relative to the centre of mass [..., n, 3]."""
+        x = np.asarray(x, dtype=np.float64)
+        xi = x.reshape(*x.shape[:-1], self.n - 1, 3)
+        return np.einsum("ik,...kd->...id", self.B, xi)
+
+    def potential_numpy(self, x):
+        pos = self.jacobi_to_positions(x)
+        v = 0.0
+        for (a, b) in self.pairs:
+            rr = np.linalg.norm(pos[..., a, :] - pos[..., b, :], axis=-1)
+            v = v + lm2m2_numpy(rr)[0]
+        return v
+
+    def initial_paths(self, walkers: int, N: int, rng, side=(3.0, 5.0), noise=0.1):
+        """Paths [walkers, DOF*N] (DOF-major): for n = 3 a random equilateral triangle of
+        side U(side) with random orientation, otherwise random points on a sphere with the
+        same nearest-neighbour scale; plus N(0, noise) Angstrom per slice and coordinate."""
+        n = self.n
+        L = rng.uniform(side[0], side[1], size=walkers)
+        if n == 3:
+            base = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.5, np.sqrt(3) / 2, 0.0]])
+        else:
+            g = rng.standard_normal((n, 3))
+            base = g / np.linalg.norm(g, axis=1, keepdims=True) * (0.5 * np.sqrt(n))
+        base = base - base.mean(axis=0)
+        q = rng.standard_normal((walkers, 4))
+        q /= np.linalg.norm(q, axis=1, keepdims=True)
+        w, x, y, z = q.T
+        R = np.stack([
+            np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+            np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+            np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1)], 1)
+        r0 = np.einsum("wij,nj->wni", R, base) * L[:, None, None]  # [walkers, n, 3]
+        r = r0[:, None, :, :] + rng.normal(0.0, noise, size=(walkers, N, n, 3))
+        xi = self.positions_to_jacobi(r)  # [walkers, N, DOF]
+        return np.ascontiguousarray(np.transpose(xi, (0, 2, 1)).reshape(walkers, self.DOF * N))

@@ -1,0 +1,189 @@
+/*
+ * feynsimul.h -- C ABI of libfeynsimul_gb300.so, the GB300 (sm_103a) engine behind the
+ * FeynSimul plugin API (physical_systems / KernelArgs / PIMCKernel / modN).
+ *
+ * Plain C types only.  Every call returns FS_OK (0) or a negative status; the handle's
+ * last error string (fs_last_error) says what went wrong.  One handle per host thread;
+ * calls on a handle are ordered on its CUDA stream.  The library owns all device memory
+ * and copies host buffers in and out, so callers keep ownership of theirs.
+ *
+ * Reference interface each call replaces (file:line in the FeynSimul tree):
+ *   fs_create ............ PIMCKernel.__init__          FeynSimul/kernel.py:53-457
+ *   fs_compile_only ...... Program.build of __init__    FeynSimul/kernel.py:372-381
+ *   fs_destroy ........... (PyOpenCL buffer release)    FeynSimul/kernel.py:386-457
+ *   fs_run ............... PIMCKernel.run               FeynSimul/kernel.py:459-506
+ *   fs_sync .............. PIMCKernel._queue.finish / kernelObj.wait   kernel.py:500, pimc_utils.py:187
+ *   fs_ranlux_init ....... PIMCKernel.initRanlux        FeynSimul/kernel.py:508-530
+ *   fs_ranlux_group_init . PIMCKernel.groupInitRanlux   FeynSimul/kernel.py:532-554
+ *   fs_set_paths ......... PIMCKernel.setPaths          FeynSimul/kernel.py:567-574
+ *   fs_get_paths ......... PIMCKernel.getPaths          FeynSimul/kernel.py:557-565
+ *   fs_get_operators ..... PIMCKernel.getOperators (raw per-thread means)   kernel.py:576-606
+ *   fs_get_correlator .... PIMCKernel.getCorrelator (raw sums)              kernel.py:608-617
+ *   fs_get_bins .......... PIMCKernel.getBinCounts (raw counts)             kernel.py:619-637
+ *   fs_get_accepts ....... PIMCKernel.getAcceptanceRate (raw counts)        kernel.py:648-658
+ *   fs_get_run_time ...... PIMCKernel.getRunTime        FeynSimul/kernel.py:638-646
+ *   fs_build_log ......... PIMCKernel.getBuildLog       FeynSimul/kernel.py:778-785
+ *   fs_source ............ the verbose cleaned.c dump   FeynSimul/kernel.py:351-364
+ *   fs_query ............. PIMCKernel.getStats / exceedsLimits / getGlobalMemory  kernel.py:660-775
+ *   fs_set_xorshift_seeds / fs_get_xorshift_seeds ... the seeds buffer  kernel.py:421-426
+ *   fs_rng_ranlux_stream / fs_rng_xorshift_stream ... the stream kernels of
+ *                                      examples/ranlux_test_kernel.c:90-161, :182-212
+ */
+#ifndef FEYNSIMUL_GB300_H
+#define FEYNSIMUL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FS_OK 0
+#define FS_ERR_CONFIG (-1)   /* invalid run parameters (kernel.py:93-211 checks) */
+#define FS_ERR_COMPILE (-2)  /* NVRTC rejected the plugin code; see fs_build_log */
+#define FS_ERR_OOM (-3)      /* device allocation failed (kernel.py:455-457) */
+#define FS_ERR_LAUNCH (-4)   /* kernel launch or execution failed */
+#define FS_ERR_TIMEOUT (-5)  /* fs_sync_timeout expired before the work finished */
+#define FS_ERR_IO (-6)       /* host buffer size mismatch */
+#define FS_ERR_CUDA (-7)     /* any other CUDA runtime error */
+#define FS_ERR_STATE (-8)    /* call not valid for this handle's configuration */
+
+/* accumulation of operator / correlator running sums */
+#define FS_ACCUM_REF_FP32 0  /* FP32 sums in the reference's order (kernel.c:622, :784) */
+#define FS_ACCUM_FP64 1      /* FP64 sums (default) */
+#define FS_ACCUM_KAHAN 2     /* compensated FP32 sums */
+#define FS_ACCUM_STUDY 3     /* FP32, Kahan-FP32 and FP64 sums side by side */
+
+typedef struct fs_handle fs_handle;
+
+/* Run parameters: the fields of KernelArgs (FeynSimul/kernel_args.py:23-51) that reach
+ * the device, plus this library's additions (marked "new"). */
+typedef struct fs_config {
+    int32_t dof;                          /* system.DOF */
+    int32_t n_slices;                     /* N (power of two) */
+    int32_t bisection_level;              /* S (2^S <= N) */
+    double beta;                          /* beta; epsilon = beta / N */
+    int32_t n_walkers;                    /* nbrOfWalkers */
+    int32_t walkers_per_group;            /* nbrOfWalkersPerWorkGroup (thread-id layout) */
+    int32_t operator_runs;                /* operatorRuns */
+    int32_t metro_steps_per_operator_run; /* metroStepsPerOperatorRun */
+    int32_t enable_parallelize_path;      /* enableParallelizePath */
+    int32_t enable_ranlux;                /* enableRanlux */
+    int32_t luxury_factor;                /* luxuaryFactor as the user gives it (kernel uses +1) */
+    uint64_t ranlux_int_max;              /* ranluxIntMax as the user gives it (kernel uses +1) */
+    int32_t enable_double;                /* enableDouble */
+    int32_t enable_bins;                  /* enableBins */
+    double x_min, x_max;                  /* xMin, xMax */
+    int32_t bin_resolution_per_dof;       /* binResolutionPerDOF */
+    /* new: histogram of plugin expressions (e.g. pair distances), shared bins */
+    double hist_lo, hist_hi;
+    int32_t hist_bins;
+    /* new: 1 = reference-compatible RNG use (see DESIGN), 0 = fixed */
+    int32_t compat;
+    /* new: FS_ACCUM_* */
+    int32_t accum;
+    /* new: 1 = fast math intrinsics (the reference builds with -cl-fast-relaxed-math);
+     * 0 = IEEE functions and no FMA contraction in plugin code (parity builds) */
+    int32_t fast_math;
+    /* new: walkers per CTA (0 = automatic) */
+    int32_t walkers_per_block;
+} fs_config;
+
+/* fs_query output */
+typedef struct fs_info {
+    int64_t n_threads;          /* reference work-items (walkers * N / 2^S, or walkers) */
+    int64_t threads_per_walker;
+    int64_t walkers_per_block;
+    int64_t block_threads;
+    int64_t grid_blocks;
+    int64_t smem_bytes;         /* dynamic shared memory per CTA */
+    int64_t registers;          /* registers per thread of the sweep kernel */
+    int64_t device_bytes;       /* device memory held by the handle */
+    int64_t uniforms_per_move;  /* 2 * DOF * (2^S - 1) + 1 */
+    int64_t nodes_per_move;     /* 2^S - 1 */
+} fs_info;
+
+/* Build the sweep for one configuration: validates, generates the CUDA source from the
+ * plugin strings, compiles it with NVRTC for sm_103a and allocates the buffers (paths
+ * zero-initialised, like kernel.py:387-389). */
+int fs_create(const fs_config *cfg, const char *potential, const char *user_code,
+              const char *const *operators, int32_t n_operators,
+              const char *const *correlators, int32_t n_correlators,
+              const char *const *histograms, int32_t n_histograms, fs_handle **out);
+int fs_destroy(fs_handle *h);
+
+/* Validate and compile only (no GPU needed): generates the CUDA source and compiles it
+ * for sm_103a; the NVRTC log (with ptxas resource usage) or the error goes to log. */
+int fs_compile_only(const fs_config *cfg, const char *potential, const char *user_code,
+                    const char *const *operators, int32_t n_operators,
+                    const char *const *correlators, int32_t n_correlators,
+                    const char *const *histograms, int32_t n_histograms, char *log,
+                    size_t log_capacity);
+
+/* Last error of the handle, or of the calling thread's last failed fs_create when h is
+ * NULL.  The pointer stays valid until the next call on the handle / thread. */
+const char *fs_last_error(const fs_handle *h);
+const char *fs_build_log(const fs_handle *h);
+const char *fs_source(const fs_handle *h);
+int fs_query(const fs_handle *h, fs_info *info);
+
+/* Paths in the reference layout: [walkers][DOF][N], float (double when enable_double). */
+int fs_set_paths(fs_handle *h, const void *host, size_t n_elems);
+int fs_get_paths(fs_handle *h, void *host, size_t n_elems);
+
+/* xorshift tables: per-thread rows [n_threads + 1][4]; per-walker rows [n_walkers][4]
+ * (the walker integer streams of the fixed mode). */
+int fs_set_xorshift_seeds(fs_handle *h, const uint32_t *rows, size_t n_rows);
+int fs_get_xorshift_seeds(fs_handle *h, uint32_t *rows, size_t n_rows);
+int fs_set_walker_seeds(fs_handle *h, const uint32_t *rows, size_t n_rows);
+int fs_get_walker_seeds(fs_handle *h, uint32_t *rows, size_t n_rows);
+
+/* RANLUX tables (28 words per row, the reference's ranluxcl_state_t layout): row i is
+ * seeded by ranluxcl_init from xs[i].  Per-thread table: n_threads rows.  Group table:
+ * n_threads rows in compat mode, n_walkers rows otherwise. */
+int fs_ranlux_init(fs_handle *h, const uint64_t *xs, size_t n_rows);
+int fs_ranlux_group_init(fs_handle *h, const uint64_t *xs, size_t n_rows);
+int fs_get_ranlux_tables(fs_handle *h, uint32_t *tab, size_t n_tab_rows, uint32_t *group_tab,
+                         size_t n_group_rows);
+int fs_set_ranlux_tables(fs_handle *h, const uint32_t *tab, size_t n_tab_rows,
+                         const uint32_t *group_tab, size_t n_group_rows);
+
+/* One reference run() = operator_runs x metro_steps_per_operator_run sweeps, launched
+ * n_launches times back to back.  Asynchronous. */
+int fs_run(fs_handle *h, int32_t n_launches);
+int fs_sync(fs_handle *h);
+int fs_sync_timeout(fs_handle *h, double seconds);
+
+/* Raw device results.  Operators: [n_threads][n_ops] per-thread means (FP32 values for
+ * FS_ACCUM_REF_FP32 / FS_ACCUM_KAHAN in FP32 builds, else FP64; [..][3] FP64 for
+ * FS_ACCUM_STUDY), returned as double.  Correlator: [walkers][n_corr][N/2] running sums
+ * since creation / the last fs_zero_accumulators, as double.  Bins: [res^DOF] counts.
+ * Histogram: [hist_bins] counts. */
+int fs_get_operators(fs_handle *h, double *out, size_t n);
+int fs_get_correlator(fs_handle *h, double *out, size_t n);
+int fs_get_accepts(fs_handle *h, uint32_t *out, size_t n);
+int fs_get_bins(fs_handle *h, uint32_t *out, size_t n);
+int fs_get_histogram(fs_handle *h, uint64_t *out, size_t n);
+int fs_zero_accumulators(fs_handle *h);
+/* device time of the last fs_run call (all its launches), seconds */
+int fs_get_run_time(fs_handle *h, double *seconds);
+
+/* Stand-alone generator streams (RNG parity tests): RANLUX: n_streams streams seeded from
+ * xs[], n_calls 4-value calls each -> out[n_streams][4*n_calls] and the final 28-word
+ * states.  lux_in_kernel is the luxury level the generator sees (luxuaryFactor + 1).
+ * xorshift: n_draws integers and floats per 4-word state; states are advanced. */
+int fs_rng_ranlux_stream(int32_t lux_in_kernel, const uint64_t *xs, int32_t n_streams,
+                         int32_t n_calls, float *out, uint32_t *states);
+int fs_rng_ranlux_stream64(int32_t lux_in_kernel, const uint64_t *xs, int32_t n_streams,
+                           int32_t n_calls, double *out);
+int fs_rng_xorshift_stream(uint32_t *states, int32_t n_streams, int32_t n_draws,
+                           uint32_t *out, float *fout);
+
+/* Library version string. */
+const char *fs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,113 @@
+"""The C-ABI boundary without a GPU: the library builds for sm_103a, loads, exports every
+symbol include/feynsimul.h declares, and the NVRTC path compiles plugin code (the OpenCL
+spellings and single-precision literals of the reference's plugins) for sm_103a."""
+import ctypes
+import os
+import re
+import types
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _lib():
+    from feynsimul_gb300 import build, _lib
+    build.build()
+    return _lib
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "feynsimul.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fs_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_exports_match_header():
+    L = _lib()
+    syms = header_symbols()
+    assert set(syms) == set(L.EXPORTS)
+    so = ctypes.CDLL(L.LIB_PATH)
+    for s in syms:
+        assert hasattr(so, s), s
+    assert b"sm_103a" in L.lib().fs_version()
+
+
+def _cfg(**kw):
+    import __graft_entry__ as g
+    return g._ho_config(**kw)
+
+
+def _compile(cfg, pot, uc="", ops=(), cors=(), hists=()):
+    L = _lib()
+    o, no = L.strings(ops)
+    c, nc = L.strings(cors)
+    h, nh = L.strings(hists)
+    buf = ctypes.create_string_buffer(1 << 16)
+    rc = L.lib().fs_compile_only(ctypes.byref(cfg), pot.encode(), uc.encode(), o, no, c, nc, h, nh,
+                                 buf, len(buf))
+    return rc, buf.value.decode(errors="replace")
+
+
+@pytest.mark.parametrize("kw", [
+    dict(),
+    dict(enable_ranlux=1, compat=1, accum=0, fast_math=0, enable_bins=1),
+    dict(enable_parallelize_path=0, walkers_per_group=1),
+    dict(enable_double=1, accum=3),
+    dict(n_slices=2048, bisection_level=2, n_walkers=4),   # 512 threads per walker
+])
+def test_nvrtc_compiles_for_sm103a(kw):
+    rc, log = _compile(_cfg(**kw), "0.5 * 1.0 * x1 * x1", "FLOAT_TYPE sqr(FLOAT_TYPE x){return x*x;}",
+                       ("1.0 * x1 * x1", "native_exp(-sqr(x1))"), ("x1",))
+    assert rc == 0, log
+    assert "fs_metropolis" in log
+
+
+def test_lm2m2_plugin_compiles():
+    from feynsimul_gb300.physical_systems.lm2m2 import Lm2m2Cluster
+    s = Lm2m2Cluster(4, 0.5)
+    rc, log = _compile(_cfg(dof=s.DOF, n_slices=64, bisection_level=3, beta=s.beta, enable_ranlux=1,
+                            hist_lo=0.0, hist_hi=20.0, hist_bins=200),
+                       s.potential, s.userCode, (s.energyOp, s.meanSquaredRadiusOp), (), s.pairDistanceOps)
+    assert rc == 0, log
+
+
+def test_compile_error_is_reported():
+    rc, log = _compile(_cfg(), "0.5 * x1 * undefined_thing")
+    assert rc == -2 and "undefined_thing" in log
+
+
+@pytest.mark.parametrize("kw,msg", [
+    (dict(n_slices=100), "power of 2"),
+    (dict(bisection_level=9), "2^S"),
+    (dict(n_walkers=10, walkers_per_group=4), "multiple"),
+    (dict(enable_ranlux=1, luxury_factor=7), "luxuaryFactor"),
+])
+def test_config_errors(kw, msg):
+    rc, log = _compile(_cfg(**kw), "x1")
+    assert rc == -1 and msg in log
+
+
+def test_python_validation_matches_reference_messages():
+    from feynsimul_gb300.kernel import PIMCKernel
+    from feynsimul_gb300.kernel_args import KernelArgs
+    sysm = types.SimpleNamespace(DOF=1, potential="x1*x1", userCode="")
+    base = dict(system=sysm, nbrOfWalkers=4, N=16, beta=1.0, S=2, enableOperator=False,
+                enableCorrelator=False, enableBisection=True, enablePathShift=False,
+                enableSingleNodeMove=False, enableBins=False, nbrOfWalkersPerWorkGroup=1,
+                enableParallelizePath=True, enableGlobalPath=False, enableGlobalOldPath=False,
+                operatorRuns=1, metroStepsPerOperatorRun=1)
+    with pytest.raises(TypeError, match="beta need to be a float"):
+        PIMCKernel(KernelArgs(**dict(base, beta=1)))
+    with pytest.raises(Exception, match="power of 2"):
+        PIMCKernel(KernelArgs(**dict(base, N=12)))
+    with pytest.raises(NameError, match="operators need to be set"):
+        PIMCKernel(KernelArgs(**dict(base, enableOperator=True)))
+    with pytest.raises(Exception, match="Single node move not possible"):
+        PIMCKernel(KernelArgs(**dict(base, enableSingleNodeMove=True, alpha=0.1)))
+
+
+def test_float_literal_rewrite_in_generated_source():
+    rc, log = _compile(_cfg(), "0.5 * x1 * x1 + 1e-3 + 2. * .25 + 0x1p-3")
+    assert rc == 0, log
