@@ -31,7 +31,7 @@ EXPORTS = (
     "fs_get_ranlux_tables", "fs_set_ranlux_tables", "fs_run", "fs_sync", "fs_sync_timeout",
     "fs_get_operators", "fs_get_correlator", "fs_get_accepts", "fs_get_bins", "fs_get_histogram",
     "fs_zero_accumulators", "fs_get_run_time", "fs_rng_ranlux_stream", "fs_rng_ranlux_stream64",
-    "fs_rng_xorshift_stream", "fs_version",
+    "fs_rng_xorshift_stream", "fs_version", "fs_ranlux_init_noalloc",
 )
 
 
@@ -104,6 +104,7 @@ _PROTOS = {
     "fs_rng_ranlux_stream": ([_I, _P, _I, _I, _P, _P], ctypes.c_int),
     "fs_rng_ranlux_stream64": ([_I, _P, _I, _I, _P], ctypes.c_int),
     "fs_rng_xorshift_stream": ([_P, _I, _I, _P, _P], ctypes.c_int),
+    "fs_ranlux_init_noalloc": ([_P, _P, _S, _P], ctypes.c_int),
 }
 
 

@@ -85,6 +85,12 @@ static int fail(fs_handle *h, int code, const char *fmt, ...)
     return code;
 }
 
+// error reporting for the library's other translation units (not exported)
+__attribute__((visibility("hidden"))) int fsi_thread_error(int code, const char *msg)
+{
+    return fail(nullptr, code, "%s", msg);
+}
+
 #define CUDA_TRY(h, call, code)                                                              \
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \

@@ -180,6 +180,20 @@ int fs_rng_ranlux_stream64(int32_t lux_in_kernel, const uint64_t *xs, int32_t n_
 int fs_rng_xorshift_stream(uint32_t *states, int32_t n_streams, int32_t n_draws,
                            uint32_t *out, float *fout);
 
+/* Seed a caller-owned RANLUX table without any device allocation: row i of table
+ * (28 uint32 words per row, device memory) is seeded by ranluxcl_init from xs[i] (host or
+ * device memory), exactly as fs_ranlux_init seeds a handle's table.  No counterpart in the
+ * reference: it is for callers that cannot let a library call cudaMalloc (hosts whose
+ * memory pool owns all device memory, bindings whose allocator must own every buffer).
+ * The seed values are staged in a fixed 2 MiB scratch array inside the library (held on
+ * every GPU that loads it until exit), so n_rows is limited to 262144 per call; larger
+ * n_rows fail with FS_ERR_CONFIG.  Asynchronous on stream (a cudaStream_t; NULL for the
+ * default stream): synchronise before reading the table.  xs may be reused when the call
+ * returns only if it is pageable host memory.  Calls share the scratch array, so calls
+ * that can overlap on the GPU race.  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture. */
+int fs_ranlux_init_noalloc(uint32_t *table, const uint64_t *xs, size_t n_rows, void *stream);
+
 /* Library version string. */
 const char *fs_version(void);
 
