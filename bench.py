@@ -73,6 +73,17 @@ def initial_paths(sysm, ka, seed):
     return np.zeros((ka["nbrOfWalkers"], ka["N"] * sysm.DOF), np.float32)
 
 
+def workload_overrides(args):
+    o = {}
+    if args.walkers:
+        o["walkers"] = args.walkers
+    if args.op_runs:
+        o["op_runs"] = args.op_runs
+    if args.msteps:
+        o["msteps"] = args.msteps
+    return o
+
+
 def node_updates_per_run(ka):
     seg = 2 ** ka["S"]
     tpw = ka["N"] // seg
@@ -260,7 +271,7 @@ def run_gb300(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     setup = he3_setup if args.config == "he3" else ho_setup
-    sysm, ka, extra, workload = setup()
+    sysm, ka, extra, workload = setup(**workload_overrides(args))
     ka_obj = KernelArgs(system=sysm, seed=1000 + rank, **extra, **ka)
     k = PIMCKernel(ka_obj)
     paths0 = initial_paths(sysm, ka, 17 + rank)
@@ -364,6 +375,9 @@ def main():
     ap.add_argument("--config", default="he3", choices=["he3", "ho"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--walkers", type=int, default=0, help="override the walker count (small cases)")
+    ap.add_argument("--op-runs", type=int, default=0, help="override operatorRuns per launch")
+    ap.add_argument("--msteps", type=int, default=0, help="override metroStepsPerOperatorRun")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -374,7 +388,7 @@ def main():
         if rank != 0:
             return
         setup = he3_setup if args.config == "he3" else ho_setup
-        sysm, ka, extra, workload = setup()
+        sysm, ka, extra, workload = setup(**workload_overrides(args))
         vals = []
         for _ in range(args.warmup):
             oracle_cpu_rate(sysm, ka, extra, seconds=1.0)
