@@ -220,6 +220,11 @@ def integrated_autocorr(series):
     return max(tau, 0.5)
 
 
+# register budget the sweep kernel is compiled for, per workload (launch-shape sweep on GB300)
+TUNED_MIN_BLOCKS = {"he3": 4, "ho": 0}
+TUNED_WPB = {"he3": 8, "ho": 0}
+
+
 # ------------------------------------------------------------------ roofline
 # Algorithmic lane operations per node update (one interior slice, all DOF, resampled by a
 # bisection move), counted from the algorithm, not from the executed code:
@@ -272,7 +277,10 @@ def run_gb300(args, rank, world):
     torch.cuda.set_device(dev)
     setup = he3_setup if args.config == "he3" else ho_setup
     sysm, ka, extra, workload = setup(**workload_overrides(args))
-    ka_obj = KernelArgs(system=sysm, seed=1000 + rank, **extra, **ka)
+    minb = args.minb if args.minb >= 0 else TUNED_MIN_BLOCKS.get(args.config, 0)
+    wpb = args.wpb if args.wpb > 0 else TUNED_WPB.get(args.config, 0)
+    ka_obj = KernelArgs(system=sysm, seed=1000 + rank, walkersPerBlock=wpb,
+                        minBlocksPerSM=minb, **extra, **ka)
     k = PIMCKernel(ka_obj)
     paths0 = initial_paths(sysm, ka, 17 + rank)
     k.setPaths(paths0)
@@ -378,6 +386,8 @@ def main():
     ap.add_argument("--walkers", type=int, default=0, help="override the walker count (small cases)")
     ap.add_argument("--op-runs", type=int, default=0, help="override operatorRuns per launch")
     ap.add_argument("--msteps", type=int, default=0, help="override metroStepsPerOperatorRun")
+    ap.add_argument("--wpb", type=int, default=0, help="walkers per thread block (0 = automatic)")
+    ap.add_argument("--minb", type=int, default=-1, help="thread blocks per SM to compile for (-1 = tuned default)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -47,7 +47,7 @@ class FsConfig(ctypes.Structure):
         ("bin_resolution_per_dof", ctypes.c_int32),
         ("hist_lo", ctypes.c_double), ("hist_hi", ctypes.c_double), ("hist_bins", ctypes.c_int32),
         ("compat", ctypes.c_int32), ("accum", ctypes.c_int32), ("fast_math", ctypes.c_int32),
-        ("walkers_per_block", ctypes.c_int32),
+        ("walkers_per_block", ctypes.c_int32), ("min_blocks_per_sm", ctypes.c_int32),
     ]
 
 

@@ -49,6 +49,7 @@ struct fs_handle {
     std::vector<std::string> ops, cors, hists;
     // launch geometry
     int tpw = 1, seg = 1, wpb = 1, block = 1, grid = 1;
+    long long wstride = 0;
     long long n_threads = 0;
     size_t smem = 0;
     int regs = 0;
@@ -204,6 +205,39 @@ static int nskip_for(int lux)
     }
 }
 
+// The bisection widths sigma_n = sqrt(2^S eps / 2^(n+1)) (kernel.c:608-618), evaluated with
+// the same IEEE operations the reference's kernel performs in FLOAT_TYPE (eps rounded from
+// its '%1.17e' literal), emitted as exact hexadecimal constants.
+static std::string sigma_table(int S, double eps_d, bool dbl)
+{
+    std::ostringstream o;
+    o << "__constant__ FT fs_sigma[" << (S + 1) << "] = {";
+    const std::string lit = fmt17(eps_d);
+    char b[64];
+    if (dbl) {
+        const double e = strtod(lit.c_str(), nullptr);
+        const double seg = (double)(1 << S);
+        for (int i = 0; i <= S; i++) {
+            double v = i == 0 ? seg * e : std::sqrt(seg * e / (2.0 * (double)(1 << i)));
+            snprintf(b, sizeof b, "%a", v);
+            o << (i ? ", " : "") << b;
+        }
+    } else {
+        const float e = strtof(lit.c_str(), nullptr);
+        const float seg = (float)(1 << S);
+        for (int i = 0; i <= S; i++) {
+            volatile float prod = seg * e;
+            volatile float den = 2.0f * (float)(1 << i);
+            volatile float q = prod / den;
+            float v = i == 0 ? (float)prod : std::sqrt((float)q);
+            snprintf(b, sizeof b, "%a", (double)v);
+            o << (i ? ", " : "") << b << "f";
+        }
+    }
+    o << "};\n";
+    return o.str();
+}
+
 static std::string gen_prelude(bool dbl)
 {
     std::ostringstream o;
@@ -240,7 +274,9 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
     const double opnorm = 1.0 / ((double)c.operator_runs * c.n_slices * c.n_walkers / (double)h.n_threads);
     o << "#define FS_DOF " << c.dof << "\n#define FS_N " << c.n_slices << "\n#define FS_S "
       << c.bisection_level << "\n#define FS_SEG " << h.seg << "\n#define FS_TPW " << h.tpw
-      << "\n#define FS_WPB " << h.wpb << "\n#define FS_NWALKERS " << c.n_walkers
+      << "\n#define FS_WPB " << h.wpb << "\n#define FS_MINB " << c.min_blocks_per_sm
+      << "\n#define FS_WSTRIDE " << h.wstride
+      << "\n#define FS_NWALKERS " << c.n_walkers
       << "\n#define FS_WPG " << c.walkers_per_group << "\n#define FS_NWG "
       << (c.n_walkers / std::max(1, c.walkers_per_group)) << "\n#define FS_PARALLEL "
       << (c.enable_parallelize_path ? 1 : 0) << "\n#define FS_RANLUX " << (c.enable_ranlux ? 1 : 0)
@@ -269,12 +305,13 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
         o << "#define FS_HBINS 0\n";
     }
     o << "#define eps FS_EPS\n";  // kernel.c:31
+    o << sigma_table(c.bisection_level, c.beta / (double)c.n_slices, dbl);
     o << "\n// ---- random number generators ----\n" << kRngSrc << "\n";
     o << "\n// ---- plugin userCode ----\n" << cvt(user_code) << "\n";
     std::ostringstream args, at;
     for (int i = 0; i < c.dof; i++) {
         args << (i ? ", " : "") << "FT x" << (i + 1);
-        at << (i ? ", " : "") << "(P)[" << i << " * FS_N + (i)]";
+        at << (i ? ", " : "") << "FS_AT(P, " << i << ", (i))";
     }
     o << "#define FS_ARGS_AT(P, i) " << at.str() << "\n";
     o << "__device__ __forceinline__ FT fs_pot(" << args.str() << ") { return (" << cvt(potential)
@@ -443,6 +480,8 @@ static int validate(const fs_config &c, int nops, int ncor, int nhist)
     if (nops < 0 || ncor < 0 || nops > 64 || ncor > 16)
         return fail(nullptr, FS_ERR_CONFIG, "at most 64 operators and 16 correlators");
     if (c.walkers_per_block < 0) return fail(nullptr, FS_ERR_CONFIG, "walkers_per_block must be >= 0");
+    if (c.min_blocks_per_sm < 0 || c.min_blocks_per_sm > 32)
+        return fail(nullptr, FS_ERR_CONFIG, "min_blocks_per_sm must be in [0, 32]");
     return FS_OK;
 }
 
@@ -492,7 +531,14 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     h->tpw = c.enable_parallelize_path ? (c.n_slices >> c.bisection_level) : 1;
     h->n_threads = (long long)c.n_walkers * h->tpw;
     h->ft = c.enable_double ? 8 : 4;
-    const size_t per_walker = (size_t)(c.dof + (int)h->cors.size()) * c.n_slices * h->ft;
+    // padded shared-memory path (see FS_PHYS in fs_pimc.cuh): one word after every 2^S
+    // slices; the walker stride is an odd multiple of 16 words
+    const long long dstride = c.n_slices + (c.n_slices >> c.bisection_level);
+    long long wstride = (long long)c.dof * dstride;
+    wstride = ((wstride + 15) / 16) * 16;
+    if ((wstride / 16) % 2 == 0) wstride += 16;
+    h->wstride = wstride;
+    const size_t per_walker = (size_t)(wstride + (long long)h->cors.size() * c.n_slices) * h->ft;
     const size_t hist_bytes = (size_t)(c.hist_bins > 0 && !h->hists.empty() ? c.hist_bins : 0) * 4;
     if (c.walkers_per_block > 0) {
         h->wpb = c.walkers_per_block;
@@ -519,6 +565,15 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     }
     h->grid = (c.n_walkers + h->wpb - 1) / h->wpb;
     h->smem = per_walker * h->wpb + hist_bytes;
+    // Register budget: unless the caller fixes it, compile for as many CTAs per SM as shared
+    // memory admits (<= 2048 threads per SM, >= 64 registers per thread).  Without the bound
+    // the compiler spends registers freely and the large kernels drop to one CTA per SM.
+    if (h->cfg.min_blocks_per_sm == 0) {
+        long long by_smem = (227ll * 1024) / std::max<long long>(1, (long long)h->smem + 1024);
+        long long by_threads = 2048 / h->block;
+        long long by_regs = 65536 / (64ll * h->block);
+        h->cfg.min_blocks_per_sm = (int)std::max(1ll, std::min(std::min(by_smem, by_threads), by_regs));
+    }
     if (h->smem > 227 * 1024) {
         delete h;
         return fail(nullptr, FS_ERR_CONFIG,
@@ -942,12 +997,13 @@ static int rng_module(int lux, cudaLibrary_t *lib)
     std::ostringstream o;
     o << gen_prelude(false) << "#define FS_NSKIP " << nskip_for(lux) << "\n#define FS_RNG_ONLY 1\n"
       << "#define FS_N 2\n#define FS_S 0\n#define FS_SEG 1\n#define FS_TPW 1\n#define FS_WPB 1\n"
-         "#define FS_NWALKERS 1\n#define FS_WPG 1\n#define FS_NWG 1\n#define FS_PARALLEL 0\n"
+         "#define FS_NWALKERS 1\n#define FS_WPG 1\n#define FS_NWG 1\n#define FS_PARALLEL 0\n#define FS_MINB 0\n"
+         "#define FS_WSTRIDE 16\n"
          "#define FS_RANLUX 0\n#define FS_COMPAT 0\n#define FS_ACCUM 1\n#define FS_FAST 0\n"
          "#define FS_NOPS 0\n#define FS_NCOR 0\n#define FS_OPRUNS 1\n#define FS_MSTEPS 1\n"
          "#define FS_EPS 1.0f\n#define FS_OPNORM 1.0f\n#define FS_BINS 0\n#define FS_NHIST 0\n"
          "#define FS_HBINS 0\n#define FS_RIM 4.294967296E+09f\n#define FS_DOF 1\n"
-      << kRngSrc << "\n#define FS_ARGS_AT(P, i) (P)[(i)]\n"
+      << kRngSrc << "\n#define FS_ARGS_AT(P, i) (P)[(i)]\n__constant__ FT fs_sigma[1] = {0.0f};\n"
       << "__device__ FT fs_pot(FT x1) { return x1; }\n" << kPimcSrc;
     fs_handle tmp;
     std::string cubin, log;

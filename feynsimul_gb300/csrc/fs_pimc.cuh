@@ -11,9 +11,9 @@
 //     by the walker (kernel.c:709-721); walker mode is one thread per walker;
 //   * FS_WPB walkers per CTA; a walker's threads sit in one warp (TPW <= 32, synchronised
 //     by __syncwarp on the walker's lanes) or fill the CTA (TPW > 32, __syncthreads);
-//   * the walker's whole path [DOF][N] lives in shared memory for the whole launch,
-//     loaded and stored once with coalesced (float4 where aligned) copies of the
-//     reference's walker-major layout;
+//   * the walker's whole path [DOF][N] lives in shared memory for the whole launch (padded
+//     so the segment threads' accesses are free of bank conflicts), loaded and stored once
+//     with coalesced reads and writes of the reference's walker-major layout;
 //   * RNG state in registers; global accepts / seeds / operator means keep the
 //     reference's thread-id layout (kernel.c:541) so the host reductions are unchanged;
 //   * operator and correlator running sums in registers (FP64 unless the
@@ -26,6 +26,15 @@
 #define FS_BLOCK (FS_WPB * FS_TPW)
 #define FS_LPT ((FS_HALF_N + FS_TPW - 1) / FS_TPW)  // correlator lags owned per thread
 #define FS_COR_REGS (FS_LPT * FS_NCOR <= 16)
+
+// Shared-memory path layout.  Slice s of degree d of a walker sits at d * FS_DSTRIDE +
+// FS_PHYS(s) with one padding word after every 2^S slices: the segment threads of a walker
+// read slices 2^S apart, which the padding turns into 2^S + 1 words apart, an odd stride,
+// so the threads of a warp hit distinct banks.  FS_WSTRIDE (walker stride, from the host)
+// is an odd multiple of 16 words so two walkers sharing a warp use opposite bank halves.
+#define FS_PHYS(s) ((s) + ((s) >> FS_S))
+#define FS_DSTRIDE (FS_N + (FS_N >> FS_S))
+#define FS_AT(P, d, s) (P)[(d) * FS_DSTRIDE + FS_PHYS(s)]
 
 #if FS_DOUBLE
 #define FS_ADD __dadd_rn
@@ -116,7 +125,7 @@ __device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, cons
     for (int i = 1; i < FS_SEG; i++) {
         const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
 #pragma unroll
-        for (int d = 0; d < FS_DOF; d++) old[(i - 1) * FS_DOF + d] = P[d * FS_N + p];
+        for (int d = 0; d < FS_DOF; d++) old[(i - 1) * FS_DOF + d] = FS_AT(P, d, p);
     }
     FS_MOVE_UNROLL
     for (int i = 1; i < FS_SEG; i++) {
@@ -132,17 +141,27 @@ __device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, cons
             const fs_u32 m = ((fs_u32)((1 + 2 * i) * half) + start) & (FS_N - 1);
             const fs_u32 l = ((fs_u32)(i * 2 * half) + start) & (FS_N - 1);
             const fs_u32 r = ((fs_u32)((i + 1) * 2 * half) + start) & (FS_N - 1);
+#if FS_RANLUX && !FS_DOUBLE && (2 * FS_DOF) % 4 == 0
+            // the node's 2*DOF uniforms (u, v per degree) in whole generator calls
+            float uv[2 * FS_DOF];
+            g.template next_k<2 * FS_DOF>(uv);
+#pragma unroll
+            for (int d = 0; d < FS_DOF; d++) {
+                const FT u = uv[2 * d];
+                const FT v = uv[2 * d + 1];
+#else
             FS_MOVE_UNROLL
             for (int d = 0; d < FS_DOF; d++) {
                 const FT u = fs_uniform(g);
                 const FT v = fs_uniform(g);
+#endif
                 FT rz = (FT)0;
                 if (v != (FT)0) {
                     // sigma_n * sqrt(-2 log v) * sin(2 pi u), left to right (kernel.c:352-353)
                     rz = FS_MUL(FS_MUL(sig, FS_SQRT(FS_MUL((FT)-2, FS_LOG(v)))),
                                 FS_SIN(FS_MUL((FT)FS_TWO_PI, u)));
                 }
-                P[d * FS_N + m] = FS_ADD(FS_MUL((FT)0.5, FS_ADD(P[d * FS_N + l], P[d * FS_N + r])), rz);
+                FS_AT(P, d, m) = FS_ADD(FS_MUL((FT)0.5, FS_ADD(FS_AT(P, d, l), FS_AT(P, d, r))), rz);
             }
         }
     }
@@ -158,7 +177,7 @@ __device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, cons
         for (int i = 1; i < FS_SEG; i++) {
             const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
 #pragma unroll
-            for (int d = 0; d < FS_DOF; d++) P[d * FS_N + p] = old[(i - 1) * FS_DOF + d];
+            for (int d = 0; d < FS_DOF; d++) FS_AT(P, d, p) = old[(i - 1) * FS_DOF + d];
         }
         return 0;
     }
@@ -206,11 +225,20 @@ __device__ __forceinline__ void fs_kahan(float &s, float &c, float x)
 }
 
 #ifndef FS_RNG_ONLY
-extern "C" __global__ void __launch_bounds__(FS_BLOCK) fs_metropolis(FsArgs a)
+#if FS_MINB > 0
+#define FS_LAUNCH_BOUNDS __launch_bounds__(FS_BLOCK, FS_MINB)
+#else
+#define FS_LAUNCH_BOUNDS __launch_bounds__(FS_BLOCK)
+#endif
+extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 {
     extern __shared__ __align__(16) unsigned char fs_smem[];
+#if FS_RANLUX
+    __shared__ FsIStream s_istream[FS_WPB];
+    __shared__ fs_u32 s_off[FS_WPB];
+#endif
     FT *s_path = (FT *)fs_smem;                                  // [WPB][DOF*N]
-    FT *s_cor = s_path + FS_WPB * FS_DOF * FS_N;                 // [WPB][NCOR][N]
+    FT *s_cor = s_path + FS_WPB * FS_WSTRIDE;                    // [WPB][NCOR][N]
     fs_u32 *s_hist = (fs_u32 *)(s_cor + FS_WPB * FS_NCOR * FS_N);  // [HBINS]
 
     const int tid_b = threadIdx.x;
@@ -221,19 +249,14 @@ extern "C" __global__ void __launch_bounds__(FS_BLOCK) fs_metropolis(FsArgs a)
     const int n_here = min(FS_WPB, FS_NWALKERS - w0);
     const bool active = wl < n_here;
 
-    // ---- path in (coalesced) ----
+    // ---- path in (coalesced global reads; padded shared layout) ----
     {
         const size_t base = (size_t)w0 * FS_DOF * FS_N;
         const int count = n_here * FS_DOF * FS_N;
-#if !FS_DOUBLE
-        if ((FS_DOF * FS_N) % 4 == 0) {
-            const float4 *src = (const float4 *)(a.paths + base);
-            float4 *dst = (float4 *)s_path;
-            for (int i = tid_b; i < count / 4; i += FS_BLOCK) dst[i] = src[i];
-        } else
-#endif
-        {
-            for (int i = tid_b; i < count; i += FS_BLOCK) s_path[i] = a.paths[base + i];
+        for (int i = tid_b; i < count; i += FS_BLOCK) {
+            const int wi = i / (FS_DOF * FS_N), r = i - wi * (FS_DOF * FS_N);
+            const int d = r / FS_N, sl = r - d * FS_N;
+            FS_AT(s_path + wi * FS_WSTRIDE, d, sl) = a.paths[base + i];
         }
 #if FS_NHIST > 0
         for (int i = tid_b; i < FS_HBINS; i += FS_BLOCK) s_hist[i] = 0u;
@@ -250,34 +273,30 @@ extern "C" __global__ void __launch_bounds__(FS_BLOCK) fs_metropolis(FsArgs a)
 #else
 #define FS_WSYNC() __syncthreads()
 #endif
-        FT *P = s_path + wl * FS_DOF * FS_N;
+        FT *P = s_path + wl * FS_WSTRIDE;
         const int tid = fs_thread_id(w, t);
-
-        // sigma table (kernel.c:608-618)
-        FT sigma[FS_S + 1];
-        sigma[0] = FS_MUL((FT)FS_SEG, (FT)FS_EPS);
-        {
-            int twoPow = 1;
-#pragma unroll
-            for (int i = 1; i <= FS_S; i++) {
-                twoPow *= 2;
-                sigma[i] = FS_SQRT_RN(FS_DIV(FS_MUL((FT)FS_SEG, (FT)FS_EPS), FS_MUL((FT)2, (FT)twoPow)));
-            }
-        }
+        // sigma table (kernel.c:608-618), computed on the host with the same FP operations
+        const FT *sigma = fs_sigma;
 
         // ---- RNG state ----
         FsUStream fs;
-        FsIStream is;
 #if FS_RANLUX
         fs_rl_load(fs.st, a.rtab + (size_t)tid * 28);
         fs.count = 0u;
+        // The walker's offset stream: every reference work-item of the walker advances an
+        // identical copy; here one lane advances it in shared memory for the walker.
+        FsIStream &is = s_istream[wl];
+        if (t == 0) {
 #if FS_COMPAT
-        fs_rl_load(is.st, a.gtab + (size_t)tid * 28);
+            fs_rl_load(is.st, a.gtab + (size_t)tid * 28);
 #else
-        fs_rl_load(is.st, a.gtab + (size_t)w * 28);
+            fs_rl_load(is.st, a.gtab + (size_t)w * 28);
 #endif
-        is.count = 0u;
+            is.count = 0u;
+        }
+        FS_WSYNC();
 #else
+        FsIStream is;
         {
             const uint4 s4 = *(const uint4 *)(a.seeds + (size_t)tid * 4);
             fs.x = s4.x; fs.y = s4.y; fs.z = s4.z; fs.w = s4.w;
@@ -325,11 +344,17 @@ extern "C" __global__ void __launch_bounds__(FS_BLOCK) fs_metropolis(FsArgs a)
         for (int run = 0; run < FS_OPRUNS; run++) {
 #pragma unroll 1
             for (int step = 0; step < FS_MSTEPS; step++) {
+#if FS_RANLUX
+                if (t == 0) s_off[wl] = fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N);
+                FS_WSYNC();
+                const fs_u32 off = s_off[wl];
+#else
+                const fs_u32 off = fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N);
+#endif
 #if FS_PARALLEL
-                const fs_u32 off = fs_offset(is, FS_SEG);
                 const fs_u32 start = (off + (fs_u32)(FS_SEG * t)) & (FS_N - 1);
 #else
-                const fs_u32 start = fs_offset(is, FS_N);
+                const fs_u32 start = off;
 #endif
                 n_acc += (fs_u32)fs_bisect(P, start, fs, sigma);
                 FS_WSYNC();
@@ -365,7 +390,7 @@ extern "C" __global__ void __launch_bounds__(FS_BLOCK) fs_metropolis(FsArgs a)
                     int ok = 1, inc = 1, bi = 0;
 #pragma unroll
                     for (int d = 0; d < FS_DOF; d++) {
-                        const FT x = P[d * FS_N + s];
+                        const FT x = FS_AT(P, d, s);
                         if (x < (FT)FS_XMIN || x >= (FT)FS_XMAX) ok = 0;
                         bi += (int)((fs_u32)FS_MUL(FS_SUB(x, (FT)FS_XMIN), (FT)FS_INVBIN)) * inc;
                         inc *= FS_BINRES;
@@ -477,6 +502,7 @@ extern "C" __global__ void __launch_bounds__(FS_BLOCK) fs_metropolis(FsArgs a)
 #endif
 #if FS_RANLUX
         fs_rl_store(fs.st, a.rtab + (size_t)tid * 28);
+        FS_WSYNC();
 #if FS_COMPAT
         fs_rl_store(is.st, a.gtab + (size_t)tid * 28);
 #else
@@ -492,19 +518,14 @@ extern "C" __global__ void __launch_bounds__(FS_BLOCK) fs_metropolis(FsArgs a)
     }
     __syncthreads();
 
-    // ---- path out (coalesced) ----
+    // ---- path out (coalesced global writes) ----
     {
         const size_t base = (size_t)w0 * FS_DOF * FS_N;
         const int count = n_here * FS_DOF * FS_N;
-#if !FS_DOUBLE
-        if ((FS_DOF * FS_N) % 4 == 0) {
-            float4 *dst = (float4 *)(a.paths + base);
-            const float4 *src = (const float4 *)s_path;
-            for (int i = tid_b; i < count / 4; i += FS_BLOCK) dst[i] = src[i];
-        } else
-#endif
-        {
-            for (int i = tid_b; i < count; i += FS_BLOCK) a.paths[base + i] = s_path[i];
+        for (int i = tid_b; i < count; i += FS_BLOCK) {
+            const int wi = i / (FS_DOF * FS_N), r = i - wi * (FS_DOF * FS_N);
+            const int d = r / FS_N, sl = r - d * FS_N;
+            a.paths[base + i] = FS_AT(s_path + wi * FS_WSTRIDE, d, sl);
         }
 #if FS_NHIST > 0
         for (int i = tid_b; i < FS_HBINS; i += FS_BLOCK)

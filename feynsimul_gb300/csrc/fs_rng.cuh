@@ -8,11 +8,11 @@
 //  * RANLUX in the RANLUXCL v1.3.1 formulation the reference vendors
 //    (examples/pyopencl-ranluxcl.cl): subtract-with-borrow on 24 lags with the p-skip
 //    schedule, xorshift64 seeding and 32-cycle warm-up.  The lags are multiples of 2^-24 in
-//    [0, 1), so this file keeps them as 24-bit integers k (value k * 2^-24): one step is
-//    d = a - b - carry; carry = sign(d); k = d mod 2^24, three integer ops instead of the
-//    reference's five float ops, with identical results because every float operation of
-//    the reference on these values is exact.  Output floats are formed exactly as the
-//    reference forms them (small values get the next lag's bits, zero maps to 2^-48).
+//    [0, 1), so this file keeps them as integers (k << 8 for value k * 2^-24) and runs the
+//    subtract-with-borrow as a hardware borrow chain (see FsRanlux); the results are
+//    identical because every float operation of the reference on these values is exact.
+//    Output floats are formed exactly as the reference forms them (small values get the
+//    next lag's bits, zero maps to 2^-48).
 //  * State tables in global memory keep the reference's 28-word float layout
 //    (pyopencl-ranluxcl.cl:264-277), converted on load and store.
 #pragma once
@@ -47,54 +47,130 @@ __device__ __forceinline__ double fs_xs_double(FsXorshift &s)
 }
 
 // ---------------------------------------------------------------- RANLUX
+// Lag value k (0 <= k < 2^24, value k * 2^-24) is held as k << 8.  Then one
+// subtract-with-borrow step s_a = s_j - s_a - c is a single `subc.cc.u32` on the shifted
+// words: the hardware borrow-out equals the digit borrow (the low bytes are zero) and the
+// top 24 bits of the difference are the new digit; an `and` clears the low byte.  Steps are
+// chained through the carry flag inside one asm block, so a step costs two instructions and
+// its critical path is one.  The borrow enters the chain as `0 - c` and leaves it as
+// `(0 - 0 - borrow) & 1`, i.e. only through subtractions, whichever polarity the flag has.
 struct FsRanlux {
-    fs_u32 s[24];   // lag value k, s[0] is the reference's s01
+    fs_u32 s[24];   // k << 8; s[0] is the reference's s01
     fs_u32 carry;   // 0 or 1 (the reference stores 0 or 2^-24)
     fs_u32 in24;
     fs_u32 stepnr;
     fs_u32 dummy;   // padding word of the table, carried through unchanged
 };
 
-// one subtract-with-borrow step on lag A (cycle position 23-A)
-template <int A>
-__device__ __forceinline__ void fs_rl_swb(FsRanlux &r)
+// cycle position p updates lag a = 23 - p from lag (a + 10) % 24
+__device__ __forceinline__ void fs_rl_chunk4_p0(FsRanlux &r)
 {
-    fs_u32 d = r.s[(A + 10) % 24] - r.s[A] - r.carry;
-    r.carry = d >> 31;
-    r.s[A] = d & 0xFFFFFFu;
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
+        "subc.cc.u32 %23, %9, %23;\n\t" "and.b32 %23, %23, -256;\n\t"
+        "subc.cc.u32 %22, %8, %22;\n\t" "and.b32 %22, %22, -256;\n\t"
+        "subc.cc.u32 %21, %7, %21;\n\t" "and.b32 %21, %21, -256;\n\t"
+        "subc.cc.u32 %20, %6, %20;\n\t" "and.b32 %20, %20, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
+        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
 }
 
-template <int A>
-__device__ __forceinline__ float fs_rl_out(FsRanlux &r)
+__device__ __forceinline__ void fs_rl_chunk4_p4(FsRanlux &r)
 {
-    fs_rl_swb<A>(r);
-    fs_u32 v = r.s[A];
-    float out = __fmul_rn(__uint2float_rn(v), 0x1p-24f);
-    if (v < 4096u) {  // value below 2^-12: add the next lag scaled by 2^-24
-        out = __fadd_rn(out, __fmul_rn(__uint2float_rn(r.s[(A + 9) % 24]), 0x1p-48f));
-        if (out == 0.0f) out = 0x1p-48f;
-    }
-    return out;
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
+        "subc.cc.u32 %19, %5, %19;\n\t" "and.b32 %19, %19, -256;\n\t"
+        "subc.cc.u32 %18, %4, %18;\n\t" "and.b32 %18, %18, -256;\n\t"
+        "subc.cc.u32 %17, %3, %17;\n\t" "and.b32 %17, %17, -256;\n\t"
+        "subc.cc.u32 %16, %2, %16;\n\t" "and.b32 %16, %16, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
+        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
 }
 
-// steps at cycle positions P..P+3 (no outputs)
-template <int P>
-__device__ __forceinline__ void fs_rl_skip4(FsRanlux &r)
+__device__ __forceinline__ void fs_rl_chunk4_p8(FsRanlux &r)
 {
-    fs_rl_swb<23 - P>(r);
-    fs_rl_swb<22 - P>(r);
-    fs_rl_swb<21 - P>(r);
-    fs_rl_swb<20 - P>(r);
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
+        "subc.cc.u32 %15, %1, %15;\n\t" "and.b32 %15, %15, -256;\n\t"
+        "subc.cc.u32 %14, %0, %14;\n\t" "and.b32 %14, %14, -256;\n\t"
+        "subc.cc.u32 %13, %23, %13;\n\t" "and.b32 %13, %13, -256;\n\t"
+        "subc.cc.u32 %12, %22, %12;\n\t" "and.b32 %12, %12, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
+        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
+}
+
+__device__ __forceinline__ void fs_rl_chunk4_p12(FsRanlux &r)
+{
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
+        "subc.cc.u32 %11, %21, %11;\n\t" "and.b32 %11, %11, -256;\n\t"
+        "subc.cc.u32 %10, %20, %10;\n\t" "and.b32 %10, %10, -256;\n\t"
+        "subc.cc.u32 %9, %19, %9;\n\t" "and.b32 %9, %9, -256;\n\t"
+        "subc.cc.u32 %8, %18, %8;\n\t" "and.b32 %8, %8, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
+        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
+}
+
+__device__ __forceinline__ void fs_rl_chunk4_p16(FsRanlux &r)
+{
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
+        "subc.cc.u32 %7, %17, %7;\n\t" "and.b32 %7, %7, -256;\n\t"
+        "subc.cc.u32 %6, %16, %6;\n\t" "and.b32 %6, %6, -256;\n\t"
+        "subc.cc.u32 %5, %15, %5;\n\t" "and.b32 %5, %5, -256;\n\t"
+        "subc.cc.u32 %4, %14, %4;\n\t" "and.b32 %4, %4, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
+        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
+}
+
+__device__ __forceinline__ void fs_rl_chunk4_p20(FsRanlux &r)
+{
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
+        "subc.cc.u32 %3, %13, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
+        "subc.cc.u32 %2, %12, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
+        "subc.cc.u32 %1, %11, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
+        "subc.cc.u32 %0, %10, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
+        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
 }
 
 __device__ __forceinline__ void fs_rl_cycle(FsRanlux &r)
 {
-    fs_rl_skip4<0>(r);
-    fs_rl_skip4<4>(r);
-    fs_rl_skip4<8>(r);
-    fs_rl_skip4<12>(r);
-    fs_rl_skip4<16>(r);
-    fs_rl_skip4<20>(r);
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
+        "subc.cc.u32 %23, %9, %23;\n\t" "and.b32 %23, %23, -256;\n\t"
+        "subc.cc.u32 %22, %8, %22;\n\t" "and.b32 %22, %22, -256;\n\t"
+        "subc.cc.u32 %21, %7, %21;\n\t" "and.b32 %21, %21, -256;\n\t"
+        "subc.cc.u32 %20, %6, %20;\n\t" "and.b32 %20, %20, -256;\n\t"
+        "subc.cc.u32 %19, %5, %19;\n\t" "and.b32 %19, %19, -256;\n\t"
+        "subc.cc.u32 %18, %4, %18;\n\t" "and.b32 %18, %18, -256;\n\t"
+        "subc.cc.u32 %17, %3, %17;\n\t" "and.b32 %17, %17, -256;\n\t"
+        "subc.cc.u32 %16, %2, %16;\n\t" "and.b32 %16, %16, -256;\n\t"
+        "subc.cc.u32 %15, %1, %15;\n\t" "and.b32 %15, %15, -256;\n\t"
+        "subc.cc.u32 %14, %0, %14;\n\t" "and.b32 %14, %14, -256;\n\t"
+        "subc.cc.u32 %13, %23, %13;\n\t" "and.b32 %13, %13, -256;\n\t"
+        "subc.cc.u32 %12, %22, %12;\n\t" "and.b32 %12, %12, -256;\n\t"
+        "subc.cc.u32 %11, %21, %11;\n\t" "and.b32 %11, %11, -256;\n\t"
+        "subc.cc.u32 %10, %20, %10;\n\t" "and.b32 %10, %10, -256;\n\t"
+        "subc.cc.u32 %9, %19, %9;\n\t" "and.b32 %9, %9, -256;\n\t"
+        "subc.cc.u32 %8, %18, %8;\n\t" "and.b32 %8, %8, -256;\n\t"
+        "subc.cc.u32 %7, %17, %7;\n\t" "and.b32 %7, %7, -256;\n\t"
+        "subc.cc.u32 %6, %16, %6;\n\t" "and.b32 %6, %6, -256;\n\t"
+        "subc.cc.u32 %5, %15, %5;\n\t" "and.b32 %5, %5, -256;\n\t"
+        "subc.cc.u32 %4, %14, %4;\n\t" "and.b32 %4, %4, -256;\n\t"
+        "subc.cc.u32 %3, %13, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
+        "subc.cc.u32 %2, %12, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
+        "subc.cc.u32 %1, %11, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
+        "subc.cc.u32 %0, %10, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
+        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
+}
+
+// output of the step that just updated lag A (pyopencl-ranluxcl.cl:363-378)
+template <int A>
+__device__ __forceinline__ float fs_rl_value(const FsRanlux &r)
+{
+    const fs_u32 v = r.s[A];
+    float out = __fmul_rn(__uint2float_rn(v), 0x1p-32f);
+    if (v < (4096u << 8)) {  // value below 2^-12: add the next lag scaled by 2^-24
+        out = __fadd_rn(out, __fmul_rn(__uint2float_rn(r.s[(A + 9) % 24]), 0x1p-56f));
+        if (out == 0.0f) out = 0x1p-48f;
+    }
+    return out;
 }
 
 // NSKIP steps starting at cycle position pos (a multiple of 4); returns the new position
@@ -104,11 +180,11 @@ __device__ __forceinline__ fs_u32 fs_rl_skip(FsRanlux &r, fs_u32 pos)
     if (NSKIP == 0) return pos;
     // up to the cycle boundary (falls through on purpose)
     switch (pos) {
-    case 4: fs_rl_skip4<4>(r);
-    case 8: fs_rl_skip4<8>(r);
-    case 12: fs_rl_skip4<12>(r);
-    case 16: fs_rl_skip4<16>(r);
-    case 20: fs_rl_skip4<20>(r);
+    case 4: fs_rl_chunk4_p4(r);
+    case 8: fs_rl_chunk4_p8(r);
+    case 12: fs_rl_chunk4_p12(r);
+    case 16: fs_rl_chunk4_p16(r);
+    case 20: fs_rl_chunk4_p20(r);
     default: break;
     }
     const int initial = pos ? 24 - (int)pos : 0;
@@ -116,25 +192,32 @@ __device__ __forceinline__ fs_u32 fs_rl_skip(FsRanlux &r, fs_u32 pos)
     const int rem = NSKIP - initial - bulk * 24;
 #pragma unroll 1
     for (int i = 0; i < bulk; i++) fs_rl_cycle(r);
-    if (rem > 0) fs_rl_skip4<0>(r);
-    if (rem > 4) fs_rl_skip4<4>(r);
-    if (rem > 8) fs_rl_skip4<8>(r);
-    if (rem > 12) fs_rl_skip4<12>(r);
-    if (rem > 16) fs_rl_skip4<16>(r);
+    if (rem > 0) fs_rl_chunk4_p0(r);
+    if (rem > 4) fs_rl_chunk4_p4(r);
+    if (rem > 8) fs_rl_chunk4_p8(r);
+    if (rem > 12) fs_rl_chunk4_p12(r);
+    if (rem > 16) fs_rl_chunk4_p16(r);
     return (fs_u32)rem;
 }
+
+#define FS_RL_OUT4(P)                          \
+    fs_rl_chunk4_p##P(r);                      \
+    o0 = fs_rl_value<23 - P>(r);               \
+    o1 = fs_rl_value<22 - P>(r);               \
+    o2 = fs_rl_value<21 - P>(r);               \
+    o3 = fs_rl_value<20 - P>(r);
 
 // four outputs (ranluxcl32), then the skip after every 24 outputs
 template <int NSKIP>
 __device__ __forceinline__ void fs_rl_next4(FsRanlux &r, float &o0, float &o1, float &o2, float &o3)
 {
     switch (r.stepnr) {
-    case 0: o0 = fs_rl_out<23>(r); o1 = fs_rl_out<22>(r); o2 = fs_rl_out<21>(r); o3 = fs_rl_out<20>(r); break;
-    case 4: o0 = fs_rl_out<19>(r); o1 = fs_rl_out<18>(r); o2 = fs_rl_out<17>(r); o3 = fs_rl_out<16>(r); break;
-    case 8: o0 = fs_rl_out<15>(r); o1 = fs_rl_out<14>(r); o2 = fs_rl_out<13>(r); o3 = fs_rl_out<12>(r); break;
-    case 12: o0 = fs_rl_out<11>(r); o1 = fs_rl_out<10>(r); o2 = fs_rl_out<9>(r); o3 = fs_rl_out<8>(r); break;
-    case 16: o0 = fs_rl_out<7>(r); o1 = fs_rl_out<6>(r); o2 = fs_rl_out<5>(r); o3 = fs_rl_out<4>(r); break;
-    default: o0 = fs_rl_out<3>(r); o1 = fs_rl_out<2>(r); o2 = fs_rl_out<1>(r); o3 = fs_rl_out<0>(r); break;
+    case 0: FS_RL_OUT4(0) break;
+    case 4: FS_RL_OUT4(4) break;
+    case 8: FS_RL_OUT4(8) break;
+    case 12: FS_RL_OUT4(12) break;
+    case 16: FS_RL_OUT4(16) break;
+    default: FS_RL_OUT4(20) break;
     }
     fs_u32 pos = r.stepnr + 4u;
     if (NSKIP % 24 == 0) {
@@ -166,14 +249,14 @@ __device__ __forceinline__ void fs_rl_seed(FsRanlux &r, fs_u64 x)
             w[k] = x;
         }
         // 192 bits w0|w1|w2, most significant first, in chunks of 24
-        r.s[b * 8 + 0] = (fs_u32)(w[0] >> 40);
-        r.s[b * 8 + 1] = (fs_u32)(w[0] >> 16) & 0xFFFFFFu;
-        r.s[b * 8 + 2] = ((fs_u32)(w[0] & 0xFFFFu) << 8) | (fs_u32)(w[1] >> 56);
-        r.s[b * 8 + 3] = (fs_u32)(w[1] >> 32) & 0xFFFFFFu;
-        r.s[b * 8 + 4] = (fs_u32)(w[1] >> 8) & 0xFFFFFFu;
-        r.s[b * 8 + 5] = ((fs_u32)(w[1] & 0xFFu) << 16) | (fs_u32)(w[2] >> 48);
-        r.s[b * 8 + 6] = (fs_u32)(w[2] >> 24) & 0xFFFFFFu;
-        r.s[b * 8 + 7] = (fs_u32)w[2] & 0xFFFFFFu;
+        r.s[b * 8 + 0] = (fs_u32)(w[0] >> 40) << 8;
+        r.s[b * 8 + 1] = ((fs_u32)(w[0] >> 16) & 0xFFFFFFu) << 8;
+        r.s[b * 8 + 2] = (((fs_u32)(w[0] & 0xFFFFu) << 8) | (fs_u32)(w[1] >> 56)) << 8;
+        r.s[b * 8 + 3] = ((fs_u32)(w[1] >> 32) & 0xFFFFFFu) << 8;
+        r.s[b * 8 + 4] = ((fs_u32)(w[1] >> 8) & 0xFFFFFFu) << 8;
+        r.s[b * 8 + 5] = (((fs_u32)(w[1] & 0xFFu) << 16) | (fs_u32)(w[2] >> 48)) << 8;
+        r.s[b * 8 + 6] = ((fs_u32)(w[2] >> 24) & 0xFFFFFFu) << 8;
+        r.s[b * 8 + 7] = ((fs_u32)w[2] & 0xFFFFFFu) << 8;
     }
     r.in24 = 0u;
     r.stepnr = 0u;
@@ -187,7 +270,7 @@ __device__ __forceinline__ void fs_rl_seed(FsRanlux &r, fs_u64 x)
 __device__ __forceinline__ void fs_rl_load(FsRanlux &r, const fs_u32 *t)
 {
 #pragma unroll
-    for (int i = 0; i < 24; i++) r.s[i] = (fs_u32)__fmul_rn(__uint_as_float(t[i]), 16777216.0f);
+    for (int i = 0; i < 24; i++) r.s[i] = (fs_u32)__fmul_rn(__uint_as_float(t[i]), 4294967296.0f);
     r.carry = t[24] != 0u ? 1u : 0u;
     r.dummy = t[25];
     r.in24 = t[26];
@@ -197,7 +280,7 @@ __device__ __forceinline__ void fs_rl_load(FsRanlux &r, const fs_u32 *t)
 __device__ __forceinline__ void fs_rl_store(const FsRanlux &r, fs_u32 *t)
 {
 #pragma unroll
-    for (int i = 0; i < 24; i++) t[i] = __float_as_uint(__fmul_rn(__uint2float_rn(r.s[i]), 0x1p-24f));
+    for (int i = 0; i < 24; i++) t[i] = __float_as_uint(__fmul_rn(__uint2float_rn(r.s[i]), 0x1p-32f));
     t[24] = r.carry ? __float_as_uint(0x1p-24f) : 0u;
     t[25] = r.dummy;
     t[26] = r.in24;
@@ -218,6 +301,53 @@ struct FsRanluxStream {
         if (c == 0u) fs_rl_next4<NSKIP>(st, b0, b1, b2, b3);
         count++;
         return c == 0u ? b0 : (c == 1u ? b1 : (c == 2u ? b2 : b3));
+    }
+
+    // K consecutive values (K a multiple of 4), the same values next() would return K
+    // times: the rem still-buffered values first, then K/4 fresh quadruples, the last rem
+    // of which stay buffered.  One branch per K values instead of one per value.
+    template <int K>
+    __device__ __forceinline__ void next_k(float (&u)[K])
+    {
+        static_assert(K % 4 == 0, "K must be a multiple of 4");
+        const fs_u32 rem = (4u - (count & 3u)) & 3u;
+        // one inlined generator call in a rolled loop (the generator is large; K/4 inlined
+        // copies cost instruction-cache misses): each quadruple is shifted in at the end
+        float c[K];
+#pragma unroll 1
+        for (int q = 0; q < K / 4; q++) {
+            float o0, o1, o2, o3;
+            fs_rl_next4<NSKIP>(st, o0, o1, o2, o3);
+#pragma unroll
+            for (int k = 0; k < K - 4; k++) c[k] = c[k + 4];
+            c[K - 4] = o0; c[K - 3] = o1; c[K - 2] = o2; c[K - 1] = o3;
+        }
+        switch (rem) {
+        case 0:
+#pragma unroll
+            for (int k = 0; k < K; k++) u[k] = c[k];
+            b0 = c[K - 4]; b1 = c[K - 3]; b2 = c[K - 2]; b3 = c[K - 1];
+            break;
+        case 1:
+            u[0] = b3;
+#pragma unroll
+            for (int k = 1; k < K; k++) u[k] = c[k - 1];
+            b3 = c[K - 1];
+            break;
+        case 2:
+            u[0] = b2; u[1] = b3;
+#pragma unroll
+            for (int k = 2; k < K; k++) u[k] = c[k - 2];
+            b2 = c[K - 2]; b3 = c[K - 1];
+            break;
+        default:
+            u[0] = b1; u[1] = b2; u[2] = b3;
+#pragma unroll
+            for (int k = 3; k < K; k++) u[k] = c[k - 3];
+            b1 = c[K - 3]; b2 = c[K - 2]; b3 = c[K - 1];
+            break;
+        }
+        count += K;
     }
 };
 

@@ -192,6 +192,7 @@ class PIMCKernel:
         c.accum = _ACCUM[self._accumulation]
         c.fast_math = int(self._fastMath)
         c.walkers_per_block = self._walkersPerBlock
+        c.min_blocks_per_sm = int(getattr(ka, "minBlocksPerSM", 0) or 0)
         self._cfg = c
 
         L = lib()

@@ -15,6 +15,8 @@ Keyword-only additions of this engine:
 * ``histograms`` / ``histRange`` / ``histBins``: plugin expressions binned into one shared
   histogram (e.g. the pair distances of a cluster).
 * ``walkersPerBlock`` (0 = automatic): walkers per CUDA thread block.
+* ``minBlocksPerSM`` (0 = as many as shared memory admits): thread blocks per SM the
+  sweep kernel is compiled to fit, i.e. its register budget.
 * ``seed`` (None): master seed for the seed tables; None draws from ``np.random`` exactly
   as kernel.py:412-426 does.
 """
@@ -59,6 +61,7 @@ class KernelArgs:
                  histRange=None,
                  histBins=None,
                  walkersPerBlock=0,
+                 minBlocksPerSM=0,
                  seed=None):
         self.system = system
         self.nbrOfWalkers = nbrOfWalkers
@@ -96,4 +99,5 @@ class KernelArgs:
         self.histRange = histRange
         self.histBins = histBins
         self.walkersPerBlock = walkersPerBlock
+        self.minBlocksPerSM = minBlocksPerSM
         self.seed = seed

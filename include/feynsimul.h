@@ -88,6 +88,9 @@ typedef struct fs_config {
     int32_t fast_math;
     /* new: walkers per CTA (0 = automatic) */
     int32_t walkers_per_block;
+    /* new: CTAs per SM the sweep kernel is compiled to fit (its register budget); 0 = as
+     * many as shared memory admits, at most 2048 threads and at least 64 registers each */
+    int32_t min_blocks_per_sm;
 } fs_config;
 
 /* fs_query output */
