@@ -31,7 +31,8 @@ EXPORTS = (
     "fs_get_ranlux_tables", "fs_set_ranlux_tables", "fs_run", "fs_sync", "fs_sync_timeout",
     "fs_get_operators", "fs_get_correlator", "fs_get_accepts", "fs_get_bins", "fs_get_histogram",
     "fs_zero_accumulators", "fs_get_run_time", "fs_rng_ranlux_stream", "fs_rng_ranlux_stream64",
-    "fs_rng_xorshift_stream", "fs_version", "fs_ranlux_init_noalloc",
+    "fs_rng_xorshift_stream", "fs_version", "fs_ranlux_init_noalloc", "fs_set_correlator",
+    "fs_set_bins", "fs_set_histogram",
 )
 
 
@@ -105,6 +106,9 @@ _PROTOS = {
     "fs_rng_ranlux_stream64": ([_I, _P, _I, _I, _P], ctypes.c_int),
     "fs_rng_xorshift_stream": ([_P, _I, _I, _P, _P], ctypes.c_int),
     "fs_ranlux_init_noalloc": ([_P, _P, _S, _P], ctypes.c_int),
+    "fs_set_correlator": ([_P, _P, _S], ctypes.c_int),
+    "fs_set_bins": ([_P, _P, _S], ctypes.c_int),
+    "fs_set_histogram": ([_P, _P, _S], ctypes.c_int),
 }
 
 

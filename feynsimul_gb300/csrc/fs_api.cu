@@ -968,6 +968,32 @@ extern "C" int fs_get_histogram(fs_handle *h, uint64_t *out, size_t n)
     if (!h) return FS_ERR_CONFIG;
     return copy_out(h, out, h->d_hist, n * 8, h->n_hist * 8);
 }
+template <class T>
+static int set_widened(fs_handle *h, void *dst, const double *in, size_t n)
+{
+    std::vector<T> tmp(n + 1);
+    for (size_t i = 0; i < n; i++) tmp[i] = (T)in[i];
+    return copy_in(h, dst, tmp.data(), n * sizeof(T), n * sizeof(T));
+}
+
+extern "C" int fs_set_correlator(fs_handle *h, const double *in, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    if (n != h->n_cor_elems) return fail(h, FS_ERR_IO, "expected %zu correlator values", h->n_cor_elems);
+    if (n == 0) return FS_OK;
+    return h->cor_elem == 4 ? set_widened<float>(h, h->d_cor, in, n) : set_widened<double>(h, h->d_cor, in, n);
+}
+extern "C" int fs_set_bins(fs_handle *h, const uint32_t *in, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_in(h, h->d_bins, in, n * 4, h->n_bins * 4);
+}
+extern "C" int fs_set_histogram(fs_handle *h, const uint64_t *in, size_t n)
+{
+    if (!h) return FS_ERR_CONFIG;
+    return copy_in(h, h->d_hist, in, n * 8, h->n_hist * 8);
+}
+
 extern "C" int fs_zero_accumulators(fs_handle *h)
 {
     if (!h) return FS_ERR_CONFIG;

@@ -481,6 +481,69 @@ class PIMCKernel:
               self._handle)
         self._ranlux_ready = True
 
+    # ------------------------------------------------------------------ checkpoints
+    def _config_fingerprint(self):
+        c = self._cfg
+        fields = {name: getattr(c, name) for name, _ in c._fields_}
+        strs = (self._system.potential, getattr(self._system, "userCode", ""), self._operators,
+                self._correlators, self._histograms)
+        return repr((sorted(fields.items()), strs))
+
+    def getState(self):
+        """Everything a continuation needs, as numpy arrays: paths, RNG tables, running sums,
+        and the run counter.  restoreState() on a kernel built from the same KernelArgs
+        continues bit for bit as if the run had not stopped."""
+        L = lib()
+        st = {"paths": self.getPaths(), "runs_since_zero": np.array(self._runsSinceZero),
+              "fingerprint": np.array(self._config_fingerprint())}
+        if self._enableRanlux:
+            st["ranlux_tab"], st["group_tab"] = self.getRanluxTables()
+        else:
+            st["seeds"] = self.getSeeds()
+            if not self._compat:
+                st["walker_seeds"] = self.getWalkerSeeds()
+        if self._enableCorrelator:
+            n = self._nbrOfWalkers * len(self._correlators) * (self._N // 2)
+            cor = np.empty(n, np.float64)
+            check(L.fs_get_correlator(self._handle, cor.ctypes.data, n), self._handle)
+            st["correlator"] = cor
+        if self._enableBins:
+            st["bins"] = self.getBinCountsRaw()
+        if self._histBins:
+            h = np.empty(self._histBins, np.uint64)
+            check(L.fs_get_histogram(self._handle, h.ctypes.data, self._histBins), self._handle)
+            st["histogram"] = h
+        return st
+
+    def restoreState(self, st):
+        if str(st["fingerprint"]) != self._config_fingerprint():
+            raise ValueError("checkpoint was written by a kernel with a different configuration")
+        L = lib()
+        self.setPaths(st["paths"])
+        if self._enableRanlux:
+            self.setRanluxTables(st["ranlux_tab"], st["group_tab"])
+        else:
+            self.setSeeds(st["seeds"])
+            if not self._compat:
+                self.setWalkerSeeds(st["walker_seeds"])
+        if "correlator" in st:
+            c = np.ascontiguousarray(st["correlator"], dtype=np.float64)
+            check(L.fs_set_correlator(self._handle, c.ctypes.data, c.size), self._handle)
+        if "bins" in st:
+            b = np.ascontiguousarray(st["bins"], dtype=np.uint32)
+            check(L.fs_set_bins(self._handle, b.ctypes.data, b.size), self._handle)
+        if "histogram" in st:
+            h = np.ascontiguousarray(st["histogram"], dtype=np.uint64)
+            check(L.fs_set_histogram(self._handle, h.ctypes.data, h.size), self._handle)
+        self._runsSinceZero = int(st["runs_since_zero"])
+
+    def saveCheckpoint(self, filename):
+        np.savez(filename, **self.getState())
+
+    def loadCheckpoint(self, filename):
+        with np.load(filename) as z:
+            self.restoreState({k: z[k] for k in z.files})
+
     # ------------------------------------------------------------------ info
     def getGlobalMemory(self):
         """Device memory held by this kernel, bytes (kernel.py:660-684)."""

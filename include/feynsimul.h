@@ -22,6 +22,9 @@
  *   fs_get_bins .......... PIMCKernel.getBinCounts (raw counts)             kernel.py:619-637
  *   fs_get_accepts ....... PIMCKernel.getAcceptanceRate (raw counts)        kernel.py:648-658
  *   fs_get_run_time ...... PIMCKernel.getRunTime        FeynSimul/kernel.py:638-646
+ *   fs_set_correlator / fs_set_bins / fs_set_histogram ... no reference counterpart: restore
+ *                          running sums from a checkpoint (the reference checkpoints paths
+ *                          only, pimc_utils.py:246-252)
  *   fs_build_log ......... PIMCKernel.getBuildLog       FeynSimul/kernel.py:778-785
  *   fs_source ............ the verbose cleaned.c dump   FeynSimul/kernel.py:351-364
  *   fs_query ............. PIMCKernel.getStats / exceedsLimits / getGlobalMemory  kernel.py:660-775
@@ -169,6 +172,10 @@ int fs_get_accepts(fs_handle *h, uint32_t *out, size_t n);
 int fs_get_bins(fs_handle *h, uint32_t *out, size_t n);
 int fs_get_histogram(fs_handle *h, uint64_t *out, size_t n);
 int fs_zero_accumulators(fs_handle *h);
+/* Restore running sums from a checkpoint (same shapes as the getters). */
+int fs_set_correlator(fs_handle *h, const double *in, size_t n);
+int fs_set_bins(fs_handle *h, const uint32_t *in, size_t n);
+int fs_set_histogram(fs_handle *h, const uint64_t *in, size_t n);
 /* device time of the last fs_run call (all its launches), seconds */
 int fs_get_run_time(fs_handle *h, double *seconds);
 
