@@ -32,7 +32,8 @@ EXPORTS = (
     "fs_get_operators", "fs_get_correlator", "fs_get_accepts", "fs_get_bins", "fs_get_histogram",
     "fs_zero_accumulators", "fs_get_run_time", "fs_rng_ranlux_stream", "fs_rng_ranlux_stream64",
     "fs_rng_xorshift_stream", "fs_version", "fs_ranlux_init_noalloc", "fs_set_correlator",
-    "fs_set_bins", "fs_set_histogram",
+    "fs_set_bins", "fs_set_histogram", "fs_mlp_sizes", "fs_mlp_train_step", "fs_mlp_adam",
+    "fs_mlp_pack", "fs_mlp_infer", "fs_set_learned_proposal",
 )
 
 
@@ -49,6 +50,7 @@ class FsConfig(ctypes.Structure):
         ("hist_lo", ctypes.c_double), ("hist_hi", ctypes.c_double), ("hist_bins", ctypes.c_int32),
         ("compat", ctypes.c_int32), ("accum", ctypes.c_int32), ("fast_math", ctypes.c_int32),
         ("walkers_per_block", ctypes.c_int32), ("min_blocks_per_sm", ctypes.c_int32),
+        ("learned", ctypes.c_int32),
     ]
 
 
@@ -109,6 +111,12 @@ _PROTOS = {
     "fs_set_correlator": ([_P, _P, _S], ctypes.c_int),
     "fs_set_bins": ([_P, _P, _S], ctypes.c_int),
     "fs_set_histogram": ([_P, _P, _S], ctypes.c_int),
+    "fs_mlp_sizes": ([_P, _P, _P, _P], ctypes.c_int),
+    "fs_mlp_train_step": ([_P, _P, _P, _P, _P, _I, _I, ctypes.c_float, _P, _P], ctypes.c_int),
+    "fs_mlp_adam": ([_P, _P, _P, _P, _P, _I, ctypes.c_float, _P], ctypes.c_int),
+    "fs_mlp_pack": ([_P, _P, _P, _P, _P], ctypes.c_int),
+    "fs_mlp_infer": ([_P, _P, _P, _P, _I, _P], ctypes.c_int),
+    "fs_set_learned_proposal": ([_P, _P, _S, _P, _S, ctypes.c_double], ctypes.c_int),
 }
 
 

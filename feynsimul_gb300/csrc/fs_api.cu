@@ -36,8 +36,14 @@ static const char *kRngSrc =
 static const char *kPimcSrc =
 #include "fs_pimc.inc"
     ;
+static const char *kMlpSrc =
+#include "fs_mlp.inc"
+    ;
 
 #define FS_VERSION "feynsimul_gb300 0.1 (sm_103a)"
+// sizes of the learned-proposal model (fs_mlp.cuh: 16-128-128-128-16)
+#define FS_MLP_FRAG_BYTES ((1 * 16 + 8 * 16 + 8 * 16 + 8 * 2) * 32 * 8)
+#define FS_MLP_NBIAS_FLOATS (128 * 3 + 16)
 
 // ------------------------------------------------------------------ errors
 static thread_local std::string g_thread_err;
@@ -68,6 +74,9 @@ struct fs_handle {
     void *d_ops = nullptr, *d_cor = nullptr;
     unsigned long long *d_hist = nullptr;
     int *d_status = nullptr;
+    void *d_mlp_frag = nullptr;
+    float *d_mlp_bias = nullptr;
+    double mlp_inv_scale = 1.0;
     size_t g_rows = 0;
     size_t device_bytes = 0;
 };
@@ -286,7 +295,8 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << "\n#define FS_NCOR " << h.cors.size() << "\n#define FS_OPRUNS " << c.operator_runs
       << "\n#define FS_MSTEPS " << c.metro_steps_per_operator_run << "\n#define FS_EPS "
       << lit(c.beta / (double)c.n_slices) << "\n#define FS_OPNORM " << lit(opnorm)
-      << "\n#define FS_BINS " << (c.enable_bins ? 1 : 0) << "\n#define FS_NHIST " << nhist << "\n";
+      << "\n#define FS_BINS " << (c.enable_bins ? 1 : 0) << "\n#define FS_NHIST " << nhist
+      << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n";
     {
         char b[64];
         snprintf(b, sizeof b, "%.9E", (double)(c.ranlux_int_max + 1ull));
@@ -307,6 +317,7 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
     o << "#define eps FS_EPS\n";  // kernel.c:31
     o << sigma_table(c.bisection_level, c.beta / (double)c.n_slices, dbl);
     o << "\n// ---- random number generators ----\n" << kRngSrc << "\n";
+    if (c.learned) o << "\n// ---- learned proposal network ----\n" << kMlpSrc << "\n";
     o << "\n// ---- plugin userCode ----\n" << cvt(user_code) << "\n";
     std::ostringstream args, at;
     for (int i = 0; i < c.dof; i++) {
@@ -480,6 +491,13 @@ static int validate(const fs_config &c, int nops, int ncor, int nhist)
     if (nops < 0 || ncor < 0 || nops > 64 || ncor > 16)
         return fail(nullptr, FS_ERR_CONFIG, "at most 64 operators and 16 correlators");
     if (c.walkers_per_block < 0) return fail(nullptr, FS_ERR_CONFIG, "walkers_per_block must be >= 0");
+    if (c.learned) {
+        if (!c.enable_parallelize_path || c.dof > 8 || c.bisection_level < 1 || c.enable_double)
+            return fail(nullptr, FS_ERR_CONFIG,
+                        "the learned proposal needs parallel-path mode, FP32, DOF <= 8 and S >= 1");
+        if ((c.n_slices >> c.bisection_level) > 32)
+            return fail(nullptr, FS_ERR_CONFIG, "the learned proposal needs N / 2^S <= 32");
+    }
     if (c.min_blocks_per_sm < 0 || c.min_blocks_per_sm > 32)
         return fail(nullptr, FS_ERR_CONFIG, "min_blocks_per_sm must be in [0, 32]");
     return FS_OK;
@@ -488,7 +506,8 @@ static int validate(const fs_config &c, int nops, int ncor, int nhist)
 static void free_buffers(fs_handle *h)
 {
     void *bufs[] = {h->d_paths, h->d_accepts, h->d_seeds, h->d_snap, h->d_wseeds, h->d_rtab,
-                    h->d_gtab, h->d_bins, h->d_ops, h->d_cor, h->d_hist, h->d_status};
+                    h->d_gtab, h->d_bins, h->d_ops, h->d_cor, h->d_hist, h->d_status,
+                    h->d_mlp_frag, h->d_mlp_bias};
     for (void *p : bufs)
         if (p) cudaFree(p);
 }
@@ -557,6 +576,16 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     if (h->tpw <= 32 && 32 % h->tpw != 0) {
         delete h;
         return fail(nullptr, FS_ERR_CONFIG, "internal: threads per walker must divide 32");
+    }
+    if (c.learned) {
+        // the network is evaluated warp-wide: every lane of every warp must hold a walker
+        const int wpw = 32 / h->tpw;
+        h->wpb = std::max(wpw, (h->wpb / wpw) * wpw);
+        if (c.n_walkers % wpw) {
+            delete h;
+            return fail(nullptr, FS_ERR_CONFIG, "the learned proposal needs the walker count to be a multiple of %d", wpw);
+        }
+        while (c.n_walkers % h->wpb) h->wpb -= wpw;
     }
     h->block = h->wpb * h->tpw;
     if (h->block > 1024) {
@@ -697,6 +726,10 @@ extern "C" int fs_create(const fs_config *cfg, const char *potential, const char
     CREATE_TRY(dalloc(h, (void **)&h->d_bins, h->n_bins * 4));
     CREATE_TRY(dalloc(h, (void **)&h->d_hist, h->n_hist * 8));
     CREATE_TRY(dalloc(h, (void **)&h->d_status, 16));
+    if (c.learned) {
+        CREATE_TRY(dalloc(h, &h->d_mlp_frag, (size_t)FS_MLP_FRAG_BYTES));
+        CREATE_TRY(dalloc(h, (void **)&h->d_mlp_bias, (size_t)FS_MLP_NBIAS_FLOATS * 4));
+    }
     CREATE_TRY(cu(cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"));
 #undef CREATE_TRY
     *out = h;
@@ -850,7 +883,21 @@ struct FsArgsHost {  // mirrors FsArgs in fs_pimc.cuh
     unsigned long long *hist;
     int *status;
     double opnorm;
+    const void *mlp_frag;
+    const float *mlp_bias;
+    float mlp_inv_scale;
 };
+
+extern "C" int fs_set_learned_proposal(fs_handle *h, const void *frag, size_t frag_bytes, const float *bias,
+                                       size_t n_bias, double inv_scale)
+{
+    if (!h) return FS_ERR_CONFIG;
+    if (!h->d_mlp_frag) return fail(h, FS_ERR_STATE, "handle was created without the learned proposal");
+    int rc = copy_in(h, h->d_mlp_frag, frag, frag_bytes, (size_t)FS_MLP_FRAG_BYTES);
+    if (!rc) rc = copy_in(h, h->d_mlp_bias, bias, n_bias * 4, (size_t)FS_MLP_NBIAS_FLOATS * 4);
+    if (!rc) h->mlp_inv_scale = inv_scale;
+    return rc;
+}
 
 extern "C" int fs_run(fs_handle *h, int32_t n_launches)
 {
@@ -872,6 +919,9 @@ extern "C" int fs_run(fs_handle *h, int32_t n_launches)
     a.hist = h->d_hist;
     a.status = h->d_status;
     a.opnorm = 1.0 / ((double)c.operator_runs * c.n_slices * c.n_walkers / (double)h->n_threads);
+    a.mlp_frag = h->d_mlp_frag;
+    a.mlp_bias = h->d_mlp_bias;
+    a.mlp_inv_scale = (float)h->mlp_inv_scale;
     void *args[] = {&a};
     CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), FS_ERR_CUDA);
     for (int i = 0; i < n_launches; i++) {
@@ -1024,7 +1074,7 @@ static int rng_module(int lux, cudaLibrary_t *lib)
     o << gen_prelude(false) << "#define FS_NSKIP " << nskip_for(lux) << "\n#define FS_RNG_ONLY 1\n"
       << "#define FS_N 2\n#define FS_S 0\n#define FS_SEG 1\n#define FS_TPW 1\n#define FS_WPB 1\n"
          "#define FS_NWALKERS 1\n#define FS_WPG 1\n#define FS_NWG 1\n#define FS_PARALLEL 0\n#define FS_MINB 0\n"
-         "#define FS_WSTRIDE 16\n"
+         "#define FS_WSTRIDE 16\n#define FS_LEARNED 0\n"
          "#define FS_RANLUX 0\n#define FS_COMPAT 0\n#define FS_ACCUM 1\n#define FS_FAST 0\n"
          "#define FS_NOPS 0\n#define FS_NCOR 0\n#define FS_OPRUNS 1\n#define FS_MSTEPS 1\n"
          "#define FS_EPS 1.0f\n#define FS_OPNORM 1.0f\n#define FS_BINS 0\n#define FS_NHIST 0\n"

@@ -116,9 +116,18 @@ __device__ __forceinline__ fs_u32 fs_offset(FsIStream &g, fs_u32 range)
 #define FS_MOVE_UNROLL _Pragma("unroll")
 #endif
 
-// kernel.c:258-399 on a shared-memory path P[DOF][N]
-__device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, const FT *sigma)
+// kernel.c:258-399 on a shared-memory path P[DOF][N].
+// With the learned proposal (FS_LEARNED) the level-1 midpoint is drawn from N(lmu, lsd^2)
+// instead of the free-particle bridge N(mid, sigma_1^2).  Both the forward and the reverse
+// proposal condition on the segment's endpoints, which the move does not change, and the
+// other nodes keep the free-particle proposal, whose density ratio cancels the kinetic
+// action exactly; the Metropolis-Hastings log-ratio therefore gains only, per degree of
+// freedom of that node, [(x_old - mid)^2 - (x_new - mid)^2] / (2 sigma_1^2)
+// + [z_new^2 - ((x_old - lmu) / lsd)^2] / 2, with z_new the standard normal drawn.
+__device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, const FT *sigma, const FT *lmu,
+                                         const FT *lsd)
 {
+    FT corr = (FT)0;
     FT old[FS_OLD_N];
     FT aOld = (FT)0;
 #pragma unroll
@@ -155,6 +164,19 @@ __device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, cons
                 const FT u = fs_uniform(g);
                 const FT v = fs_uniform(g);
 #endif
+#if FS_LEARNED
+                if (n == 1) {
+                    FT z = (FT)0;
+                    if (v != (FT)0) z = FS_MUL(FS_SQRT(FS_MUL((FT)-2, FS_LOG(v))), FS_SIN(FS_MUL((FT)FS_TWO_PI, u)));
+                    const FT mid = FS_MUL((FT)0.5, FS_ADD(FS_AT(P, d, l), FS_AT(P, d, r)));
+                    const FT xo = FS_AT(P, d, m);
+                    const FT xn = lmu[d] + lsd[d] * z;
+                    const FT dn = xn - mid, dov = xo - mid, zo = (xo - lmu[d]) / lsd[d];
+                    corr += (dov * dov - dn * dn) / (2 * sig * sig) + (FT)0.5 * (z * z - zo * zo);
+                    FS_AT(P, d, m) = xn;
+                    continue;
+                }
+#endif
                 FT rz = (FT)0;
                 if (v != (FT)0) {
                     // sigma_n * sqrt(-2 log v) * sin(2 pi u), left to right (kernel.c:352-353)
@@ -172,7 +194,14 @@ __device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, cons
         aNew = FS_ADD(aNew, FS_MUL((FT)FS_EPS, fs_pot(FS_ARGS_AT(P, p))));
     }
     const FT acc = fs_uniform(g);
+#if FS_LEARNED
+    if (FS_EXP(FS_SUB(aOld, aNew) + corr) < acc) {
+#else
+    (void)corr;
+    (void)lmu;
+    (void)lsd;
     if (FS_EXP(FS_SUB(aOld, aNew)) < acc) {
+#endif
 #pragma unroll
         for (int i = 1; i < FS_SEG; i++) {
             const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
@@ -198,6 +227,9 @@ struct FsArgs {
     fs_u64 *hist;              // [hist bins]
     int *status;
     double opnorm;
+    const uint2 *mlp_frag;     // learned proposal: network fragments and biases
+    const float *mlp_bias;
+    float mlp_inv_scale;       // features = endpoint coordinates * mlp_inv_scale
 };
 
 __device__ __forceinline__ int fs_thread_id(int w, int t)
@@ -356,7 +388,38 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #else
                 const fs_u32 start = off;
 #endif
-                n_acc += (fs_u32)fs_bisect(P, start, fs, sigma);
+#if FS_LEARNED
+                // level-1 proposal from the segment's endpoints (warp-wide network evaluation)
+                FT lmu[FS_DOF], lsd[FS_DOF];
+                {
+                    float feat[FS_MLP_IN], out[FS_MLP_OUT];
+#pragma unroll
+                    for (int k = 0; k < FS_MLP_IN; k++) feat[k] = 0.f;
+                    const fs_u32 e1 = (start + FS_SEG) & (FS_N - 1);
+#pragma unroll
+                    for (int d = 0; d < FS_DOF; d++) {
+                        const FT x0 = FS_AT(P, d, start), x1 = FS_AT(P, d, e1);
+                        feat[d] = 0.5f * (x0 + x1) * a.mlp_inv_scale;
+                        feat[FS_DOF + d] = 0.5f * (x1 - x0) * a.mlp_inv_scale;
+                    }
+                    fs_mlp_eval_warp(a.mlp_frag, a.mlp_bias, feat, out);
+                    const FT s1 = sigma[1];
+#pragma unroll
+                    for (int d = 0; d < FS_DOF; d++) {
+                        const FT mid = 0.5f * (FS_AT(P, d, start) + FS_AT(P, d, e1));
+                        float o = out[d], sv = 4.f * tanhf(0.25f * out[FS_DOF + d]);
+                        if (!(fabsf(o) < 64.f) || !(fabsf(sv) <= 4.f)) {  // non-finite: free proposal
+                            o = 0.f;
+                            sv = 0.f;
+                        }
+                        lmu[d] = mid + s1 * o;
+                        lsd[d] = s1 * __expf(0.5f * sv);
+                    }
+                }
+                n_acc += (fs_u32)fs_bisect(P, start, fs, sigma, lmu, lsd);
+#else
+                n_acc += (fs_u32)fs_bisect(P, start, fs, sigma, nullptr, nullptr);
+#endif
                 FS_WSYNC();
             }
             // ---- measurement (kernel.c:734-797) ----

@@ -193,6 +193,8 @@ class PIMCKernel:
         c.fast_math = int(self._fastMath)
         c.walkers_per_block = self._walkersPerBlock
         c.min_blocks_per_sm = int(getattr(ka, "minBlocksPerSM", 0) or 0)
+        c.learned = int(bool(getattr(ka, "learnedProposal", False)))
+        self._learned = bool(c.learned)
         self._cfg = c
 
         L = lib()
@@ -480,6 +482,24 @@ class PIMCKernel:
         check(lib().fs_set_ranlux_tables(self._handle, t.ctypes.data, t.shape[0], g.ctypes.data, g.shape[0]),
               self._handle)
         self._ranlux_ready = True
+
+    # ------------------------------------------------------------------ learned proposal
+    def setLearnedProposal(self, model):
+        """Load a feynsimul_gb300.learned.LearnedProposal into the sweep (the kernel must be
+        built with learnedProposal=True).  The model's sigma_1 must be this kernel's
+        level-1 bisection width."""
+        if not self._learned:
+            raise Exception("create the kernel with learnedProposal=True")
+        from .learned import sigma_level
+        s1 = sigma_level(self._beta, self._N, self._S, 1)
+        if abs(model.sigma1 - s1) > 1e-6 * s1:
+            raise ValueError(f"model was trained for sigma_1 = {model.sigma1}, this kernel has {s1}")
+        if model.dof != self._system.DOF:
+            raise ValueError("model DOF differs from the system's")
+        frag, bias = model.packed()
+        check(lib().fs_set_learned_proposal(self._handle, frag.ctypes.data, frag.nbytes, bias.ctypes.data,
+                                            bias.size, 1.0 / model.length_scale), self._handle)
+        self._model = model
 
     # ------------------------------------------------------------------ checkpoints
     def _config_fingerprint(self):

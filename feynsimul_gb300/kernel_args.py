@@ -17,6 +17,9 @@ Keyword-only additions of this engine:
 * ``walkersPerBlock`` (0 = automatic): walkers per CUDA thread block.
 * ``minBlocksPerSM`` (0 = as many as shared memory admits): thread blocks per SM the
   sweep kernel is compiled to fit, i.e. its register budget.
+* ``learnedProposal`` (False): draw each segment's level-1 midpoint from a learned Gaussian
+  (feynsimul_gb300.learned), Metropolis-Hastings corrected; load the model with
+  PIMCKernel.setLearnedProposal.
 * ``seed`` (None): master seed for the seed tables; None draws from ``np.random`` exactly
   as kernel.py:412-426 does.
 """
@@ -62,6 +65,7 @@ class KernelArgs:
                  histBins=None,
                  walkersPerBlock=0,
                  minBlocksPerSM=0,
+                 learnedProposal=False,
                  seed=None):
         self.system = system
         self.nbrOfWalkers = nbrOfWalkers
@@ -100,4 +104,5 @@ class KernelArgs:
         self.histBins = histBins
         self.walkersPerBlock = walkersPerBlock
         self.minBlocksPerSM = minBlocksPerSM
+        self.learnedProposal = learnedProposal
         self.seed = seed

@@ -1,0 +1,226 @@
+"""Learned bisection proposal: harvest, training and loading into the sampler.
+
+No counterpart in the reference.  The plain sweep proposes each bisection midpoint from
+the free-particle bridge N((x_l + x_r)/2, sigma_n^2) (FeynSimul/GPUsrc/kernel.c:306-362).
+Here a small network (16-128-128-128-16, ReLU, BF16 weights, FP32 accumulation; kernels in
+csrc/fs_mlp.cuh and csrc/fs_mlp_train.cu) predicts, for the level-1 midpoint of each
+segment, a Gaussian N(mid + sigma_1 o, sigma_1^2 exp(s)) from the segment's endpoints.
+The sweep draws from it and corrects the acceptance (Metropolis-Hastings), so the target
+distribution is exact for any network; with zero output weights the proposal is the free
+one.
+
+Workflow::
+
+    model = LearnedProposal(dof, sigma_1, length_scale)
+    x, z = harvest_triples(paths, dof, N, S, sigma_1, length_scale)   # from plain-sampler paths
+    model.train(x, z, steps=2000)                                     # GPU, own kernels
+    kernel.setLearnedProposal(model)                                  # PIMCKernel(learnedProposal=True)
+
+Features of a segment: (x_l + x_r)/2 and (x_r - x_l)/2 per degree of freedom times
+1/length_scale, zero padded to 16.  Target: z = (x_mid - (x_l + x_r)/2) / sigma_1.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+IN, H, OUT = 16, 128, 16
+SHAPES = [("W1", (H, IN)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("W3", (H, H)), ("b3", (H,)),
+          ("W4", (OUT, H)), ("b4", (OUT,))]
+
+
+def param_count():
+    return sum(int(np.prod(s)) for _, s in SHAPES)
+
+
+def unflatten(params):
+    out, o = {}, 0
+    for name, shp in SHAPES:
+        n = int(np.prod(shp))
+        out[name] = params[o:o + n].reshape(shp)
+        o += n
+    return out
+
+
+def to_bf16(x):
+    """Round float32 values to BF16 (nearest even), returned as float32 values."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+def bf16_bits(x):
+    return (to_bf16(x).view(np.uint32) >> 16).astype(np.uint16)
+
+
+def pack_fragments(params):
+    """FP32 parameters -> (fragment-ordered BF16 weights as uint32 pairs, biases) in the
+    layout fs_mlp_eval_warp reads (csrc/fs_mlp.cuh)."""
+    p = unflatten(np.asarray(params, dtype=np.float32))
+    blobs = []
+    for name in ("W1", "W2", "W3", "W4"):
+        W = p[name]                      # [N][K]
+        N, K = W.shape
+        kt, nt, lane = np.meshgrid(np.arange(K // 16), np.arange(N // 8), np.arange(32), indexing="ij")
+        n = nt * 8 + lane // 4
+        k = kt * 16 + (lane % 4) * 2
+        lo0, hi0 = bf16_bits(W[n, k]), bf16_bits(W[n, k + 1])
+        lo1, hi1 = bf16_bits(W[n, k + 8]), bf16_bits(W[n, k + 9])
+        x = lo0.astype(np.uint32) | (hi0.astype(np.uint32) << 16)
+        y = lo1.astype(np.uint32) | (hi1.astype(np.uint32) << 16)
+        blobs.append(np.stack([x, y], axis=-1).reshape(-1, 2))   # order (kt, nt, lane)
+    frag = np.ascontiguousarray(np.concatenate(blobs, axis=0))
+    bias = np.ascontiguousarray(np.concatenate([p["b1"], p["b2"], p["b3"], p["b4"]]).astype(np.float32))
+    return frag, bias
+
+
+def init_params(seed=0, zero_output=True):
+    """He-initialised hidden layers; the output layer starts at zero, i.e. the free proposal."""
+    rng = np.random.RandomState(seed)
+    chunks = []
+    for name, shp in SHAPES:
+        if name.startswith("b"):
+            chunks.append(np.zeros(shp, np.float32))
+        elif name == "W4" and zero_output:
+            chunks.append(np.zeros(shp, np.float32))
+        else:
+            chunks.append((rng.randn(*shp) * np.sqrt(2.0 / shp[1])).astype(np.float32))
+    return np.concatenate([c.ravel() for c in chunks]).astype(np.float32)
+
+
+def features(x_left, x_right, length_scale):
+    """(n, D) endpoints -> (n, 16) float32 features."""
+    xl = np.asarray(x_left, dtype=np.float64)
+    xr = np.asarray(x_right, dtype=np.float64)
+    n, d = xl.shape
+    f = np.zeros((n, IN), np.float32)
+    f[:, :d] = 0.5 * (xl + xr) / length_scale
+    f[:, d:2 * d] = 0.5 * (xr - xl) / length_scale
+    return f
+
+
+def harvest_triples(paths, dof, N, S, sigma1, length_scale, per_walker=None, rng=None):
+    """Training data from equilibrium paths [walkers, DOF*N]: every segment start p gives the
+    endpoints x[p], x[p + 2^S] and the level-1 midpoint x[p + 2^(S-1)] (periodic).  Returns
+    (features [n, 16], targets z [n, 8])."""
+    P = np.asarray(paths, dtype=np.float64).reshape(paths.shape[0], dof, N)
+    seg = 2 ** S
+    rng = rng or np.random.RandomState(0)
+    W = P.shape[0]
+    starts = np.arange(N) if per_walker is None else None
+    if per_walker is None:
+        w_idx = np.repeat(np.arange(W), N)
+        p_idx = np.tile(starts, W)
+    else:
+        w_idx = np.repeat(np.arange(W), per_walker)
+        p_idx = rng.randint(0, N, size=W * per_walker)
+    xl = P[w_idx, :, p_idx]
+    xm = P[w_idx, :, (p_idx + seg // 2) % N]
+    xr = P[w_idx, :, (p_idx + seg) % N]
+    feats = features(xl, xr, length_scale)
+    z = np.zeros((xl.shape[0], 8), np.float32)
+    z[:, :dof] = (xm - 0.5 * (xl + xr)) / sigma1
+    return feats, z
+
+
+def sigma_level(beta, N, S, n):
+    """Free-particle bisection width at level n (kernel.c:608-618), in FP64."""
+    return float(np.sqrt((2 ** S) * (beta / N) / (2.0 * 2 ** n)))
+
+
+class LearnedProposal:
+    """The network's parameters plus the constants that tie it to a system and a level."""
+
+    def __init__(self, dof, sigma1, length_scale, params=None, seed=0):
+        if not 1 <= dof <= 8:
+            raise ValueError("the learned proposal supports 1 <= DOF <= 8")
+        self.dof = dof
+        self.sigma1 = float(sigma1)
+        self.length_scale = float(length_scale)
+        self.params = init_params(seed) if params is None else np.asarray(params, np.float32).copy()
+        self.history = []
+
+    # ---- packing for the sampler ----
+    def packed(self):
+        return pack_fragments(self.params)
+
+    def save(self, filename):
+        np.savez(filename, params=self.params, dof=self.dof, sigma1=self.sigma1,
+                 length_scale=self.length_scale)
+
+    @classmethod
+    def load(cls, filename):
+        z = np.load(filename)
+        return cls(int(z["dof"]), float(z["sigma1"]), float(z["length_scale"]), params=z["params"])
+
+    # ---- evaluation on the GPU with the sampler's device code ----
+    def predict(self, feats):
+        """Raw network outputs (n, 16) for features (n, 16), via fs_mlp_infer."""
+        import torch
+        L = _lib.lib()
+        frag, bias = self.packed()
+        dev = "cuda"
+        tf = torch.from_numpy(frag.view(np.uint8).copy()).to(dev)
+        tb = torch.from_numpy(bias).to(dev)
+        tx = torch.from_numpy(np.ascontiguousarray(feats, np.float32)).to(dev)
+        ty = torch.zeros((tx.shape[0], OUT), dtype=torch.float32, device=dev)
+        s = torch.cuda.current_stream().cuda_stream
+        _lib.check(L.fs_mlp_infer(tf.data_ptr(), tb.data_ptr(), tx.data_ptr(), ty.data_ptr(), tx.shape[0], s))
+        torch.cuda.synchronize()
+        return ty.cpu().numpy()
+
+    def conditional(self, feats):
+        """(mean shift o, std factor exp(s/2)) per DOF, in units of sigma_1."""
+        y = self.predict(feats)
+        o = y[:, :self.dof]
+        s = 4.0 * np.tanh(0.25 * y[:, self.dof:2 * self.dof])
+        return o, np.exp(0.5 * s)
+
+    # ---- training on the GPU with the project's kernels ----
+    def train(self, feats, targets, steps=2000, batch=4096, lr=1e-3, seed=0, log_every=0):
+        """Adam on the Gaussian negative log-likelihood; returns the loss history (per step,
+        mean over the batch)."""
+        import torch
+        L = _lib.lib()
+        dev = "cuda"
+        n = feats.shape[0]
+        batch = min(batch, n)
+        sizes = [ctypes.c_int64() for _ in range(4)]
+        _lib.check(L.fs_mlp_sizes(*[ctypes.byref(v) for v in sizes]))
+        n_param, n_bf16 = sizes[0].value, sizes[1].value
+        assert n_param == self.params.size
+        tp = torch.from_numpy(self.params.copy()).to(dev)
+        tm = torch.zeros_like(tp)
+        tv = torch.zeros_like(tp)
+        tg = torch.zeros_like(tp)
+        tq = torch.zeros(n_bf16, dtype=torch.int16, device=dev)
+        frag_dummy = torch.zeros(sizes[2].value * 2, dtype=torch.int32, device=dev)
+        bias_dummy = torch.zeros(sizes[3].value, dtype=torch.float32, device=dev)
+        tx = torch.from_numpy(np.ascontiguousarray(feats, np.float32)).to(dev)
+        tz = torch.from_numpy(np.ascontiguousarray(targets, np.float32)).to(dev)
+        loss = torch.zeros(1, dtype=torch.float32, device=dev)
+        stream = torch.cuda.current_stream().cuda_stream
+        _lib.check(L.fs_mlp_pack(tp.data_ptr(), tq.data_ptr(), frag_dummy.data_ptr(), bias_dummy.data_ptr(), stream))
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(seed)
+        losses = torch.zeros(steps, dtype=torch.float32, device=dev)
+        for it in range(steps):
+            idx = torch.randint(0, n, (batch,), device=dev, generator=gen)
+            xb = tx.index_select(0, idx).contiguous()
+            zb = tz.index_select(0, idx).contiguous()
+            loss.zero_()
+            _lib.check(L.fs_mlp_train_step(tp.data_ptr(), tq.data_ptr(), tg.data_ptr(), xb.data_ptr(),
+                                           zb.data_ptr(), batch, self.dof, 1.0 / batch, loss.data_ptr(), stream))
+            _lib.check(L.fs_mlp_adam(tp.data_ptr(), tm.data_ptr(), tv.data_ptr(), tg.data_ptr(), tq.data_ptr(),
+                                     it + 1, lr, stream))
+            losses[it] = loss[0] / batch
+            if log_every and (it + 1) % log_every == 0:
+                print(f"step {it + 1}: loss {float(losses[it]):.4f}")
+        torch.cuda.synchronize()
+        self.params = tp.cpu().numpy().astype(np.float32)
+        hist = losses.cpu().numpy()
+        self.history.extend(hist.tolist())
+        return hist

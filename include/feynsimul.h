@@ -94,6 +94,10 @@ typedef struct fs_config {
     /* new: CTAs per SM the sweep kernel is compiled to fit (its register budget); 0 = as
      * many as shared memory admits, at most 2048 threads and at least 64 registers each */
     int32_t min_blocks_per_sm;
+    /* new: 1 = learned level-1 bisection proposal (Metropolis-Hastings corrected); needs
+     * parallel-path mode, DOF <= 8 and whole warps of walkers; the model is set with
+     * fs_set_learned_proposal (until then the network is zero, i.e. the free proposal) */
+    int32_t learned;
 } fs_config;
 
 /* fs_query output */
@@ -203,6 +207,32 @@ int fs_rng_xorshift_stream(uint32_t *states, int32_t n_streams, int32_t n_draws,
  * that can overlap on the GPU race.  The first call on a device looks up the array's
  * device address; make that first call before any stream capture. */
 int fs_ranlux_init_noalloc(uint32_t *table, const uint64_t *xs, size_t n_rows, void *stream);
+
+/* ---- learned bisection proposal (no counterpart in the reference) ----
+ * A 16-128-128-128-16 ReLU network (BF16 weights, FP32 accumulation on the tensor cores)
+ * predicts, from a segment's endpoints, a Gaussian for the segment's midpoint; the sweep
+ * draws the midpoint from it and corrects the acceptance (Metropolis-Hastings), so the
+ * sampled distribution is unchanged whatever the network.  Parameters are one FP32 array
+ * of fs_mlp_sizes()->n_param floats: W1[128][16] b1 W2[128][128] b2 W3[128][128] b3
+ * W4[16][128] b4.  Training entry points take device pointers and a cudaStream_t. */
+int fs_mlp_sizes(int64_t *n_param, int64_t *n_bf16, int64_t *n_frag_u2, int64_t *n_bias);
+/* One forward + backward pass over n_rows (features x[n][16], targets z[n][8]) adding the
+ * gradient of the mean loss (inv_batch = 1/batch) to grad and the loss sum to *loss. */
+int fs_mlp_train_step(const float *params, const uint16_t *wq, float *grad, const float *x,
+                      const float *z, int32_t n_rows, int32_t dof, float inv_batch, float *loss,
+                      void *stream);
+/* Adam (beta 0.9 / 0.999) on params; refreshes the BF16 copy wq; clears grad. */
+int fs_mlp_adam(float *params, float *m, float *v, float *grad, uint16_t *wq, int32_t step,
+                float lr, void *stream);
+/* params -> BF16 training copy, inference fragments (n_frag_u2 x 8 bytes), biases. */
+int fs_mlp_pack(const float *params, uint16_t *wq, void *frag, float *bias, void *stream);
+/* Inference of rows x[n][16] -> y[n][16] with the sampler's device code. */
+int fs_mlp_infer(const void *frag, const float *bias, const float *x, float *y, int32_t n_rows,
+                 void *stream);
+/* Load a packed model (host buffers) into a handle created with cfg.learned = 1;
+ * inv_scale multiplies the endpoint coordinates to form the features. */
+int fs_set_learned_proposal(fs_handle *h, const void *frag, size_t frag_bytes, const float *bias,
+                            size_t n_bias, double inv_scale);
 
 /* Library version string. */
 const char *fs_version(void);

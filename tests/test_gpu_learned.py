@@ -1,0 +1,192 @@
+"""The learned bisection proposal on the GPU: packing, inference and gradients of the
+project's tensor-core kernels against the CPU oracle (oracle/mlp_oracle.py), training on
+harmonic-oscillator paths recovering the exact Gaussian conditional, and the
+Metropolis-Hastings correction keeping the sampled distribution exact."""
+import ctypes
+import types
+
+import numpy as np
+import pytest
+
+from gpu_util import engine, require_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    require_gpu()
+    engine()
+
+
+def _rand_params(seed, out_scale=0.05):
+    from feynsimul_gb300 import learned
+    p = learned.init_params(seed, zero_output=False)
+    u = learned.unflatten(p)
+    u["W4"][...] *= out_scale
+    rng = np.random.RandomState(seed + 1)
+    for b in ("b1", "b2", "b3", "b4"):
+        u[b][...] = rng.randn(*u[b].shape) * 0.05
+    return p
+
+
+def test_pack_matches_host_layout():
+    import torch
+    from feynsimul_gb300 import _lib, learned
+    L = _lib.lib()
+    p = _rand_params(3)
+    sizes = [ctypes.c_int64() for _ in range(4)]
+    L.fs_mlp_sizes(*[ctypes.byref(v) for v in sizes])
+    tp = torch.from_numpy(p).cuda()
+    tq = torch.zeros(sizes[1].value, dtype=torch.int16, device="cuda")
+    tf = torch.zeros(sizes[2].value * 2, dtype=torch.int32, device="cuda")
+    tb = torch.zeros(sizes[3].value, dtype=torch.float32, device="cuda")
+    _lib.check(L.fs_mlp_pack(tp.data_ptr(), tq.data_ptr(), tf.data_ptr(), tb.data_ptr(), None))
+    torch.cuda.synchronize()
+    frag, bias = learned.pack_fragments(p)
+    assert np.array_equal(tf.cpu().numpy().view(np.uint32).reshape(-1, 2), frag)
+    assert np.array_equal(tb.cpu().numpy(), bias)
+    u = learned.unflatten(p)
+    want_q = np.concatenate([learned.bf16_bits(u[w]).ravel() for w in ("W1", "W2", "W3", "W4")])
+    assert np.array_equal(tq.cpu().numpy().view(np.uint16), want_q)
+
+
+def test_inference_matches_oracle():
+    from feynsimul_gb300.learned import LearnedProposal
+    from oracle import mlp_oracle
+    p = _rand_params(5, out_scale=0.3)
+    m = LearnedProposal(6, 0.2, 1.0, params=p)
+    x = np.random.RandomState(1).randn(1000, 16).astype(np.float32)
+    x[:, 12:] = 0
+    y = m.predict(x)
+    _, _, _, z4 = mlp_oracle.forward(p, x)
+    np.testing.assert_allclose(y, z4, rtol=2e-2, atol=2e-2 * np.abs(z4).max())
+
+
+def test_gradients_match_oracle():
+    import torch
+    from feynsimul_gb300 import _lib
+    from oracle import mlp_oracle
+    L = _lib.lib()
+    p = _rand_params(7, out_scale=0.3)
+    rng = np.random.RandomState(2)
+    B, dof = 256, 6
+    x = rng.randn(B, 16).astype(np.float32)
+    x[:, 2 * dof:] = 0
+    z = np.zeros((B, 8), np.float32)
+    z[:, :dof] = rng.randn(B, dof)
+    sizes = [ctypes.c_int64() for _ in range(4)]
+    L.fs_mlp_sizes(*[ctypes.byref(v) for v in sizes])
+    tp = torch.from_numpy(p).cuda()
+    tq = torch.zeros(sizes[1].value, dtype=torch.int16, device="cuda")
+    tf = torch.zeros(sizes[2].value * 2, dtype=torch.int32, device="cuda")
+    tb = torch.zeros(sizes[3].value, dtype=torch.float32, device="cuda")
+    _lib.check(L.fs_mlp_pack(tp.data_ptr(), tq.data_ptr(), tf.data_ptr(), tb.data_ptr(), None))
+    tg = torch.zeros_like(tp)
+    tx, tz = torch.from_numpy(x).cuda(), torch.from_numpy(z).cuda()
+    tl = torch.zeros(1, dtype=torch.float32, device="cuda")
+    _lib.check(L.fs_mlp_train_step(tp.data_ptr(), tq.data_ptr(), tg.data_ptr(), tx.data_ptr(), tz.data_ptr(),
+                                   B, dof, 1.0 / B, tl.data_ptr(), None))
+    torch.cuda.synchronize()
+    loss_ref, g_ref = mlp_oracle.loss_and_grad(p, x, z, dof, 1.0 / B)
+    g = tg.cpu().numpy().astype(np.float64)
+    assert abs(float(tl.item()) - loss_ref) < 1e-3 * abs(loss_ref) + 1e-3
+    off = 0
+    for name, n in (("W1", 2048), ("b1", 128), ("W2", 16384), ("b2", 128), ("W3", 16384), ("b3", 128),
+                    ("W4", 2048), ("b4", 16)):
+        a, b = g[off:off + n], g_ref[off:off + n]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+        assert rel < 2e-2, (name, rel)
+        off += n
+
+
+def _ho_kernel(learned, N=64, S=3, walkers=2048, beta=8.0, op_runs=20, msteps=2, seed=11):
+    kernel, kernel_args = engine()
+    sysm = types.SimpleNamespace(DOF=1, potential="0.5 * 1.0 * x1 * x1", userCode="")
+    ka = kernel_args.KernelArgs(
+        system=sysm, nbrOfWalkers=walkers, N=N, beta=beta, S=S, enableOperator=True,
+        enableCorrelator=False, enableBisection=True, enablePathShift=False, enableSingleNodeMove=False,
+        enableBins=False, nbrOfWalkersPerWorkGroup=1, enableParallelizePath=True, enableGlobalPath=False,
+        enableGlobalOldPath=False, operators=("1.0 * x1 * x1",), operatorRuns=op_runs,
+        metroStepsPerOperatorRun=msteps, seed=seed, learnedProposal=learned)
+    return kernel.PIMCKernel(ka)
+
+
+def _exact_ho(beta, N, S):
+    from test_gpu_physics import exact_ho
+    h = 2 ** (S - 1)
+    x2, c = exact_ho(beta, N, [0, h, 2 * h])
+    C0, Ch, C2 = c
+    a = Ch / (C0 + C2)
+    var = C0 - 2 * Ch * Ch / (C0 + C2)
+    return x2, a, var
+
+
+def test_zero_network_equals_free_proposal():
+    from feynsimul_gb300.learned import LearnedProposal, sigma_level
+    plain = _ho_kernel(False, walkers=256)
+    lrn = _ho_kernel(True, walkers=256)
+    lrn.setLearnedProposal(LearnedProposal(1, sigma_level(8.0, 64, 3, 1), 1.0))
+    p0 = np.random.RandomState(0).randn(256, 64).astype(np.float32) * 0.5
+    for k in (plain, lrn):
+        k.setPaths(p0)
+        k.setSeeds(plain.getSeeds())
+        k.setWalkerSeeds(plain.getWalkerSeeds())
+    plain.run()
+    lrn.run()
+    # same random numbers; the correction is zero up to rounding, so decisions agree
+    # except where exp(dS) lies within rounding of its uniform
+    diff = np.abs(plain.getAccepts().astype(int) - lrn.getAccepts().astype(int)).sum()
+    assert diff <= 3, diff
+    plain.close()
+    lrn.close()
+
+
+def test_random_network_keeps_the_distribution_exact():
+    """A deliberately wrong proposal (random network) must still sample the HO exactly."""
+    from feynsimul_gb300.learned import LearnedProposal, sigma_level
+    k = _ho_kernel(True)
+    k.setLearnedProposal(LearnedProposal(1, sigma_level(8.0, 64, 3, 1), 1.0, params=_rand_params(9, out_scale=0.5)))
+    for _ in range(5):
+        k.run()
+    e = []
+    for _ in range(20):
+        k.run()
+        e.append(k.getOperators()[0].mean())
+    e = np.array(e)
+    x2, _, _ = _exact_ho(8.0, 64, 3)
+    se = e.std(ddof=1) / np.sqrt(len(e))
+    assert abs(e.mean() - x2) < 5 * se + 1e-4, (e.mean(), x2, se)
+    assert k.getAcceptanceRate() > 0.05
+    k.close()
+
+
+def test_training_recovers_ho_conditional():
+    """Train on plain-sampler HO paths; the network must learn the exact Gaussian
+    conditional of the level-1 midpoint given the endpoints."""
+    from feynsimul_gb300.learned import LearnedProposal, harvest_triples, sigma_level
+    N, S, beta = 64, 3, 8.0
+    k = _ho_kernel(False, N=N, S=S, beta=beta, walkers=4096)
+    for _ in range(5):
+        k.run()
+    feats, z = [], []
+    s1 = sigma_level(beta, N, S, 1)
+    for _ in range(4):
+        k.run()
+        f, t = harvest_triples(k.getPaths(), 1, N, S, s1, 1.0)
+        feats.append(f)
+        z.append(t)
+    k.close()
+    feats, z = np.concatenate(feats), np.concatenate(z)
+    m = LearnedProposal(1, s1, 1.0)
+    hist = m.train(feats, z, steps=1500, batch=4096, lr=2e-3)
+    assert hist[-100:].mean() < hist[:10].mean()
+    _, a, var = _exact_ho(beta, N, S)
+    mids = np.linspace(-1.0, 1.0, 21)
+    test = np.zeros((21, 16), np.float32)
+    test[:, 0] = mids
+    o, sd = m.conditional(test)
+    o_exact = (2 * a - 1) * mids / s1
+    sd_exact = np.sqrt(var) / s1
+    assert np.all(np.abs(o[:, 0] - o_exact) < 0.06 + 0.05 * np.abs(o_exact)), (o[:, 0], o_exact)
+    assert np.all(np.abs(sd[:, 0] - sd_exact) < 0.05 * sd_exact), (sd[:, 0], sd_exact)
