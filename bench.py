@@ -265,6 +265,33 @@ def roofline_for(config, ka, node_rate, clk):
                           "(MEASURED_PEAKS.json has HBM and bf16 peaks only; this kernel uses neither)"}
 
 
+# ------------------------------------------------------------------ learned vs plain
+def learned_study(quick=True):
+    """Energy-estimator ESS/s of the plain sampler and of the learned level-1 proposal on the
+    He3 workload (feynsimul_gb300.learned.ess_study).  ESS from Sokal-windowed integrated
+    autocorrelation of per-walker energies measured after every launch of 4 sweeps, all
+    samplers from the same equilibrated paths; training time is not included in ESS/s."""
+    from feynsimul_gb300 import build as fb
+    fb.build()
+    from feynsimul_gb300.learned import ess_study
+    from feynsimul_gb300.physical_systems.lm2m2 import Lm2m2Cluster
+    sysm = Lm2m2Cluster(3, 1.0)
+    t0 = time.perf_counter()
+    res = ess_study(sysm, sysm.beta, 256, 16384,
+                    S_plain=(4, 5) if quick else (3, 4, 5, 6), S_learned=(4, 5) if quick else (4, 5, 6, 7),
+                    launches=40 if quick else 60, train_steps=1500 if quick else 3000,
+                    kernel_extra=dict(enableRanlux=True, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
+                                      minBlocksPerSM=3), log=lambda *a: None)
+    out = {"metric": "energy ESS/s, learned vs plain sampler (He3 LM2M2 T=1K N=256 16384 walkers RANLUX)",
+           "summary": res["summary"], "wall_s": time.perf_counter() - t0,
+           "plain": {str(k): {kk: v[kk] for kk in ("acceptance", "tau_int_launches", "ess_per_s",
+                                                    "node_updates_per_s")} for k, v in res["plain"].items()},
+           "learned": {str(k): {kk: v[kk] for kk in ("acceptance", "tau_int_launches", "ess_per_s",
+                                                      "node_updates_per_s", "loss_start", "loss_end")}
+                       for k, v in res["learned"].items()}}
+    return out
+
+
 # ------------------------------------------------------------------ arms
 def run_gb300(args, rank, world):
     from feynsimul_gb300 import build as fb
@@ -380,7 +407,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="he3", choices=["he3", "ho"])
+    ap.add_argument("--config", default="he3", choices=["he3", "ho", "learned"])
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain ESS study")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--walkers", type=int, default=0, help="override the walker count (small cases)")
@@ -418,6 +446,10 @@ def main():
         print(json.dumps(out))
         return
 
+    if args.config == "learned":
+        if rank == 0:
+            print(json.dumps(learned_study(quick=False)))
+        return
     if world > 1:
         import torch
         import torch.distributed as dist
@@ -425,6 +457,8 @@ def main():
         dist.init_process_group("nccl")
     result, (sysm, ka, extra) = run_gb300(args, rank, world)
     if rank == 0:
+        if args.config == "he3" and not args.no_learned:
+            result["learned_vs_plain"] = learned_study(quick=True)["summary"]
         if not args.no_cpu_baseline:
             result["cpu_baseline"] = oracle_cpu_rate(sysm, ka, extra, seconds=args.cpu_seconds)
         print(json.dumps(result))

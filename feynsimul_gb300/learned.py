@@ -224,3 +224,104 @@ class LearnedProposal:
         hist = losses.cpu().numpy()
         self.history.extend(hist.tolist())
         return hist
+
+
+# ------------------------------------------------------------------ ESS study
+def energy_series(kernel, launches, op_index=0):
+    """Per-walker operator means of `launches` consecutive runs and their device time."""
+    series, t = [], 0.0
+    for _ in range(launches):
+        kernel.run()
+        t += kernel.getRunTime()
+        series.append(kernel.getOperators()[op_index])
+    return np.array(series), t
+
+
+def ess_study(system, beta, N, walkers, S_plain=(3, 4, 5, 6), S_learned=(4, 5, 6, 7), launches=60,
+              op_runs=1, msteps=4, burn=10, train_steps=3000, harvest_snapshots=4, seed=1,
+              kernel_extra=None, log=print):
+    """Energy-estimator ESS/s of the plain sampler and of the learned proposal on one
+    system.  Every sampler starts from the same equilibrated paths; a launch is op_runs x
+    msteps sweeps followed by one operator measurement per walker and run."""
+    from .kernel import PIMCKernel
+    from .kernel_args import KernelArgs
+    from .stats import ess, tau_int_batch_means
+
+    extra = dict(kernel_extra or {})
+
+    def make(S, learned, op_runs_=op_runs, msteps_=msteps):
+        ka = KernelArgs(system=system, nbrOfWalkers=walkers, N=N, beta=float(beta), S=S, enableOperator=True,
+                        enableCorrelator=False, enableBisection=True, enablePathShift=False,
+                        enableSingleNodeMove=False, enableBins=False, nbrOfWalkersPerWorkGroup=1,
+                        enableParallelizePath=True, enableGlobalPath=False, enableGlobalOldPath=False,
+                        operators=(system.energyOp,), operatorRuns=op_runs_, metroStepsPerOperatorRun=msteps_,
+                        seed=seed + 17 * S + (1000 if learned else 0), learnedProposal=learned, **extra)
+        k = PIMCKernel(ka)
+        if ka.enableRanlux:
+            k.initRanlux()
+            k.groupInitRanlux()
+        return k
+
+    rng = np.random.RandomState(seed)
+    # equilibrate with the plain sampler at the middle level
+    k0 = make(S_plain[len(S_plain) // 2], False, 5, 10)
+    if hasattr(system, "initial_paths"):
+        k0.setPaths(system.initial_paths(walkers, N, rng))
+    for _ in range(burn):
+        k0.run()
+    snaps = []
+    for _ in range(harvest_snapshots):
+        k0.run()
+        snaps.append(k0.getPaths())
+    start_paths = snaps[-1].copy()
+    k0.close()
+    length_scale = float(np.sqrt(np.mean(np.concatenate(snaps) ** 2)))
+    results = {"plain": {}, "learned": {}, "length_scale": length_scale}
+
+    def measure(k, label):
+        k.setPaths(start_paths)
+        for _ in range(3):
+            k.run()
+        series, t = energy_series(k, launches)
+        e, tau = ess(series)
+        info = k.getInfo()
+        nodes = walkers * (N // 2 ** k._S) * (2 ** k._S - 1) * op_runs * msteps * launches
+        r = {"S": k._S, "ess": e, "tau_int_launches": tau, "tau_batch_means": tau_int_batch_means(series),
+             "device_s": t, "ess_per_s": e / t, "node_updates_per_s": nodes / t,
+             "acceptance": float(k.getAcceptanceRate()), "energy_mean": float(series.mean()),
+             "energy_se": float(series.mean(axis=0).std() / np.sqrt(walkers)), "registers": int(info.registers)}
+        log(f"{label} S={k._S}: AR {r['acceptance']:.3f} tau {tau:.2f} ESS/s {r['ess_per_s']:.4g} "
+            f"nodes/s {r['node_updates_per_s']:.4g} E {r['energy_mean']:.5f}")
+        return r
+
+    for S in S_plain:
+        k = make(S, False)
+        results["plain"][S] = measure(k, "plain  ")
+        k.close()
+    for S in S_learned:
+        s1 = sigma_level(beta, N, S, 1)
+        feats, z = [], []
+        for P in snaps:
+            f, t = harvest_triples(P, system.DOF, N, S, s1, length_scale, per_walker=64, rng=rng)
+            feats.append(f)
+            z.append(t)
+        feats, z = np.concatenate(feats), np.concatenate(z)
+        model = LearnedProposal(system.DOF, s1, length_scale, seed=seed)
+        hist = model.train(feats, z, steps=train_steps, batch=8192, lr=1e-3, seed=seed)
+        k = make(S, True)
+        k.setLearnedProposal(model)
+        r = measure(k, "learned")
+        r.update(train_samples=int(feats.shape[0]), loss_start=float(hist[:20].mean()),
+                 loss_end=float(hist[-50:].mean()))
+        results["learned"][S] = r
+        k.close()
+    best_plain = max(results["plain"].values(), key=lambda r: r["ess_per_s"])
+    best_learned = max(results["learned"].values(), key=lambda r: r["ess_per_s"])
+    ref = results["plain"].get(4, best_plain)
+    results["summary"] = {
+        "plain_S4_ess_per_s": ref["ess_per_s"], "best_plain_S": best_plain["S"],
+        "best_plain_ess_per_s": best_plain["ess_per_s"], "best_learned_S": best_learned["S"],
+        "best_learned_ess_per_s": best_learned["ess_per_s"],
+        "learned_vs_plain_S4": best_learned["ess_per_s"] / ref["ess_per_s"],
+        "learned_vs_best_plain": best_learned["ess_per_s"] / best_plain["ess_per_s"]}
+    return results
