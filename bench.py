@@ -292,6 +292,40 @@ def learned_study(quick=True):
     return out
 
 
+# ------------------------------------------------------------------ ragged batch
+def batch_bench(args):
+    """64 LM2M2 systems (n U{3..10}, N in {128..1024}, T U(0.5, 2) K, walkers U{1024..8192}),
+    one persistent launch per step replayed from a CUDA graph, launch shape autotuned."""
+    from feynsimul_gb300 import build as fb
+    fb.build()
+    from feynsimul_gb300.batch import BatchSampler, autotune, ragged_workload
+    wl = ragged_workload(seed=0, n_systems=64)
+    t0 = time.perf_counter()
+    tune = autotune(wl, op_runs=1, msteps=4)
+    t_tune = time.perf_counter() - t0
+    b = BatchSampler(wl, op_runs=1, msteps=4, block_threads=tune["block_threads"], tpw_target=tune["tpw_target"])
+    for _ in range(max(3, args.warmup)):
+        b.run(1)
+    steps = max(3, min(args.steps, 10))
+    t = b.run(steps, graph=True)
+    value = b.node_updates_per_launch * steps / t
+    out = {"metric": "path-node updates/s, ragged batch of 64 LM2M2 systems in one persistent launch",
+           "value": value, "unit": "node-updates/s", "n_gpus": 1, "steps": steps, "warmup": max(3, args.warmup),
+           "ms_per_step": 1e3 * t / steps, "higher_is_better": True, "dtype": "f32 (u32 RNG, f64 sums)",
+           "data": "synthetic, seeded", "config": {
+               "workload": "64 systems: n U{3..10}, N in {128,256,512,1024}, T U(0.5,2) K, walkers U{1024..8192}, "
+                           "xorshift, 4 sweeps + 1 energy measurement per step",
+               "node_updates_per_step": b.node_updates_per_launch, "work_items": b.n_items, "grid": b.grid,
+               "block_threads": tune["block_threads"], "tpw_target": tune["tpw_target"],
+               "registers": b.registers, "smem_bytes": b.smem, "cuda_graph": True},
+           "autotune": {"cached": tune["cached"], "seconds": t_tune,
+                        "candidates": [{k: c.get(k) for k in ("block_threads", "tpw_target", "node_updates_per_s",
+                                                              "error")} for c in tune.get("candidates", [])]},
+           "gpu_launches": steps}
+    b.close()
+    return out
+
+
 # ------------------------------------------------------------------ arms
 def run_gb300(args, rank, world):
     from feynsimul_gb300 import build as fb
@@ -407,7 +441,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="he3", choices=["he3", "ho", "learned"])
+    ap.add_argument("--config", default="he3", choices=["he3", "ho", "learned", "batch"])
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain ESS study")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -446,6 +480,10 @@ def main():
         print(json.dumps(out))
         return
 
+    if args.config == "batch":
+        if rank == 0:
+            print(json.dumps(batch_bench(args)))
+        return
     if args.config == "learned":
         if rank == 0:
             print(json.dumps(learned_study(quick=False)))

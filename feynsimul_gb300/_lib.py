@@ -33,7 +33,9 @@ EXPORTS = (
     "fs_zero_accumulators", "fs_get_run_time", "fs_rng_ranlux_stream", "fs_rng_ranlux_stream64",
     "fs_rng_xorshift_stream", "fs_version", "fs_ranlux_init_noalloc", "fs_set_correlator",
     "fs_set_bins", "fs_set_histogram", "fs_mlp_sizes", "fs_mlp_train_step", "fs_mlp_adam",
-    "fs_mlp_pack", "fs_mlp_infer", "fs_set_learned_proposal",
+    "fs_mlp_pack", "fs_mlp_infer", "fs_set_learned_proposal", "fs_batch_create", "fs_batch_destroy",
+    "fs_batch_run", "fs_batch_sync", "fs_batch_get_run_time", "fs_batch_set_paths", "fs_batch_get_paths",
+    "fs_batch_set_seeds", "fs_batch_get_op_sums", "fs_batch_get_accepts", "fs_batch_query",
 )
 
 
@@ -58,6 +60,12 @@ class FsInfo(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int64) for n in (
         "n_threads", "threads_per_walker", "walkers_per_block", "block_threads", "grid_blocks",
         "smem_bytes", "registers", "device_bytes", "uniforms_per_move", "nodes_per_move")]
+
+
+class FsBatchSystem(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("n_walkers", ctypes.c_int32), ("n_slices", ctypes.c_int32),
+                ("bisection_level", ctypes.c_int32), ("beta", ctypes.c_double),
+                ("walkers_per_tile", ctypes.c_int32)]
 
 
 class FsError(RuntimeError):
@@ -117,6 +125,17 @@ _PROTOS = {
     "fs_mlp_pack": ([_P, _P, _P, _P, _P], ctypes.c_int),
     "fs_mlp_infer": ([_P, _P, _P, _P, _I, _P], ctypes.c_int),
     "fs_set_learned_proposal": ([_P, _P, _S, _P, _S, ctypes.c_double], ctypes.c_int),
+    "fs_batch_create": ([_I, _P, _STRS, _STRS, _STRS, _I, _I, _P, _I, _I, _I, ctypes.POINTER(_P)], ctypes.c_int),
+    "fs_batch_destroy": ([_P], ctypes.c_int),
+    "fs_batch_run": ([_P, _I, _I], ctypes.c_int),
+    "fs_batch_sync": ([_P], ctypes.c_int),
+    "fs_batch_get_run_time": ([_P, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+    "fs_batch_set_paths": ([_P, _I, _P, _S], ctypes.c_int),
+    "fs_batch_get_paths": ([_P, _I, _P, _S], ctypes.c_int),
+    "fs_batch_set_seeds": ([_P, _I, _P, _S, _P, _S], ctypes.c_int),
+    "fs_batch_get_op_sums": ([_P, _I, _P, _S], ctypes.c_int),
+    "fs_batch_get_accepts": ([_P, _I, _P, _S], ctypes.c_int),
+    "fs_batch_query": ([_P, _P, _P, _P, _P, _P, _P, _S], ctypes.c_int),
 }
 
 

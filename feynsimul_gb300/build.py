@@ -69,7 +69,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     stamp = os.path.join(BUILD, "stamp")
     if not force and os.path.exists(LIB) and os.path.exists(stamp) and open(stamp).read() == fp:
         return LIB
-    for name in ("fs_rng.cuh", "fs_pimc.cuh", "fs_mlp.cuh"):
+    for name in ("fs_rng.cuh", "fs_pimc.cuh", "fs_mlp.cuh", "fs_batch.cuh"):
         _embed(name)
     home = _cuda_home(nvcc)
     objs = []

@@ -39,6 +39,10 @@ static const char *kPimcSrc =
 static const char *kMlpSrc =
 #include "fs_mlp.inc"
     ;
+static const char *kBatchSrc =
+#include "fs_batch.inc"
+    ;
+__attribute__((visibility("hidden"))) const char *fsi_batch_src() { return kBatchSrc; }
 
 #define FS_VERSION "feynsimul_gb300 0.1 (sm_103a)"
 // sizes of the learned-proposal model (fs_mlp.cuh: 16-128-128-128-16)
@@ -341,6 +345,21 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
 }
 
 // ------------------------------------------------------------------ NVRTC + cache
+static int compile_module(fs_handle *h, const std::string &src, bool fast, std::string *cubin, std::string *log);
+
+// internal entry points for the library's other translation units (not exported)
+__attribute__((visibility("hidden"))) std::string fsi_float_literals(const std::string &s) { return float_literals(s); }
+__attribute__((visibility("hidden"))) std::string fsi_prelude(bool dbl) { return gen_prelude(dbl); }
+__attribute__((visibility("hidden"))) const char *fsi_rng_src() { return kRngSrc; }
+__attribute__((visibility("hidden"))) const char *fsi_batch_src();
+__attribute__((visibility("hidden"))) int fsi_compile(const std::string &src, bool fast, std::string *cubin,
+                                                      std::string *log)
+{
+    fs_handle tmp;
+    int rc = compile_module(&tmp, src, fast, cubin, log);
+    if (rc) g_thread_err = tmp.err;
+    return rc;
+}
 static std::mutex g_cache_mu;
 static std::unordered_map<std::string, std::string> g_cubins;
 

@@ -1,0 +1,187 @@
+// fs_batch.cuh -- many independent systems of different sizes in one persistent launch.
+// No counterpart in the reference (which runs one system per OpenCL program).
+//
+// fs_api.cu pastes the RNG header, then for every system type k (one per distinct DOF
+// value / plugin) the plugin's code inside `namespace fs_type_k` plus a functor with the
+// potential and operators, then this file and a generated dispatcher kernel.
+//
+// A work item is a tile of walkers of one system.  CTAs pull items from a global counter
+// (largest first, so the ragged tail is short) and run all the launch's sweeps on the
+// tile: the same Metropolis-bisection move as fs_pimc.cuh (kernel.c:258-399, with the
+// fixed-mode xorshift streams), but N, S, epsilon, the bisection widths and the walker
+// counts are runtime values of the system, the path tile lives in shared memory while the
+// saved old segments go to the CTA's slice of a global scratch buffer (a 27-DOF,
+// 1024-slice walker's path alone takes 117 KB), and a walker wider than a warp
+// synchronises with a named barrier of its own.
+#pragma once
+
+#define FS_BATCH_MAX_S 10
+
+struct FsBatchSys {
+    float *paths;            // [walkers][DOF][N]
+    float *old_scratch;      // per CTA slot: saved segments [(seg-1)*DOF][tile threads]
+    fs_u32 *seeds;           // [threads][4]  (thread = walker * tpw + t)
+    fs_u32 *wseeds;          // [walkers][4]
+    fs_u32 *accepts;         // [threads]
+    double *op_sums;         // [walkers][nops], accumulated over launches
+    int n_walkers, N, S, tpw, wpb, nops, type, n_tiles;
+    int op_runs, msteps;
+    float eps;
+    float sigma[FS_BATCH_MAX_S + 1];
+};
+
+struct FsBatchItem {
+    int sys, tile;
+};
+
+__device__ __forceinline__ void fs_walker_sync(int tpw, int wl)
+{
+    if (tpw <= 32) {
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned m = tpw == 32 ? 0xFFFFFFFFu : (((1u << tpw) - 1u) << (lane / tpw * tpw));
+        __syncwarp(m);
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + wl), "r"(tpw) : "memory");
+    }
+}
+
+// One tile: walkers [tile*wpb, ...) of system sd.  All threads of the CTA call it.
+template <int DOF, class Sys>
+__device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, float *smem, size_t old_slot_floats)
+{
+    const int tid = threadIdx.x;
+    const int N = sd.N, S = sd.S, seg = 1 << S, tpw = sd.tpw;
+    const int dstride = N + (N >> S);
+    int wstride = DOF * dstride;
+    wstride = ((wstride + 15) / 16) * 16;
+    if ((wstride / 16) % 2 == 0) wstride += 16;
+    const int w0 = tile * sd.wpb;
+    const int n_here = min(sd.wpb, sd.n_walkers - w0);
+    const int wl = tid / tpw, t = tid % tpw;
+    const bool active = wl < n_here;
+    const int nthr = sd.wpb * tpw;
+    // saved old segments: this CTA's slice of the global scratch, [(seg-1)*DOF][tile threads]
+    float *s_old = sd.old_scratch + (size_t)blockIdx.x * old_slot_floats;
+    double *s_op = (double *)(smem + sd.wpb * wstride);  // [wpb][nops]
+
+#define FSB_AT(P, d, s) (P)[(d) * dstride + (s) + ((s) >> S)]
+    {
+        const size_t base = (size_t)w0 * DOF * N;
+        const int count = n_here * DOF * N;
+        for (int i = tid; i < count; i += blockDim.x) {
+            const int wi = i / (DOF * N), r = i - wi * (DOF * N);
+            const int d = r / N, sl = r - d * N;
+            FSB_AT(smem + wi * wstride, d, sl) = sd.paths[base + i];
+        }
+        for (int i = tid; i < sd.wpb * sd.nops; i += blockDim.x) s_op[i] = 0.0;
+    }
+    __syncthreads();
+
+    if (active) {
+        const int w = w0 + wl;
+        float *P = smem + wl * wstride;
+        const int th = w * tpw + t;
+        FsXorshift g, ws;
+        {
+            const uint4 s4 = *(const uint4 *)(sd.seeds + (size_t)th * 4);
+            g.x = s4.x; g.y = s4.y; g.z = s4.z; g.w = s4.w;
+            const uint4 g4 = *(const uint4 *)(sd.wseeds + (size_t)w * 4);
+            ws.x = g4.x; ws.y = g4.y; ws.z = g4.z; ws.w = g4.w;
+        }
+        fs_u32 n_acc = 0u;
+        double opd[Sys::NOPS > 0 ? Sys::NOPS : 1];
+#pragma unroll
+        for (int k = 0; k < Sys::NOPS; k++) opd[k] = 0.0;
+        const float eps = sd.eps;
+#pragma unroll 1
+        for (int run = 0; run < sd.op_runs; run++) {
+#pragma unroll 1
+            for (int step = 0; step < sd.msteps; step++) {
+                const fs_u32 off = fs_xs_next(ws) & (fs_u32)(seg - 1);
+                const int start = (int)((off + (fs_u32)(seg * t)) & (fs_u32)(N - 1));
+                // ---- bisection move (kernel.c:258-399) ----
+                float aOld = 0.f, aNew = 0.f;
+                float x[DOF];
+#pragma unroll 1
+                for (int i = 1; i < seg; i++) {
+                    const int p = (start + i) & (N - 1);
+#pragma unroll
+                    for (int d = 0; d < DOF; d++) {
+                        x[d] = FSB_AT(P, d, p);
+                        s_old[((i - 1) * DOF + d) * nthr + tid] = x[d];
+                    }
+                    aOld = __fadd_rn(aOld, __fmul_rn(eps, Sys::pot(x)));
+                }
+#pragma unroll 1
+                for (int n = 1; n <= S; n++) {
+                    const int half = 1 << (S - n);
+                    const float sig = sd.sigma[n];
+#pragma unroll 1
+                    for (int i = 0; i < (1 << (n - 1)); i++) {
+                        const int m = ((1 + 2 * i) * half + start) & (N - 1);
+                        const int l = (i * 2 * half + start) & (N - 1);
+                        const int r = ((i + 1) * 2 * half + start) & (N - 1);
+#pragma unroll
+                        for (int d = 0; d < DOF; d++) {
+                            const float u = fs_xs_float(g), v = fs_xs_float(g);
+                            float rz = 0.f;
+                            if (v != 0.f)
+                                rz = __fmul_rn(__fmul_rn(sig, sqrtf(__fmul_rn(-2.f, __logf(v)))),
+                                               __sinf(__fmul_rn(6.28318548f, u)));
+                            FSB_AT(P, d, m) = __fadd_rn(__fmul_rn(0.5f, __fadd_rn(FSB_AT(P, d, l), FSB_AT(P, d, r))), rz);
+                        }
+                    }
+                }
+#pragma unroll 1
+                for (int i = 1; i < seg; i++) {
+                    const int p = (start + i) & (N - 1);
+#pragma unroll
+                    for (int d = 0; d < DOF; d++) x[d] = FSB_AT(P, d, p);
+                    aNew = __fadd_rn(aNew, __fmul_rn(eps, Sys::pot(x)));
+                }
+                if (__expf(__fsub_rn(aOld, aNew)) < fs_xs_float(g)) {
+#pragma unroll 1
+                    for (int i = 1; i < seg; i++) {
+                        const int p = (start + i) & (N - 1);
+#pragma unroll
+                        for (int d = 0; d < DOF; d++) FSB_AT(P, d, p) = s_old[((i - 1) * DOF + d) * nthr + tid];
+                    }
+                } else {
+                    n_acc++;
+                }
+                fs_walker_sync(tpw, wl);
+            }
+            // ---- measurement: the thread's slices (kernel.c:734-745) ----
+            if (Sys::NOPS > 0) {
+#pragma unroll 1
+                for (int s = t * seg; s < (t + 1) * seg; s++) {
+                    float x[DOF], ov[Sys::NOPS > 0 ? Sys::NOPS : 1];
+#pragma unroll
+                    for (int d = 0; d < DOF; d++) x[d] = FSB_AT(P, d, s);
+                    Sys::ops(x, ov);
+#pragma unroll
+                    for (int k = 0; k < Sys::NOPS; k++) opd[k] += (double)ov[k];
+                }
+            }
+            fs_walker_sync(tpw, wl);
+        }
+        sd.accepts[th] = n_acc;
+        *(uint4 *)(sd.seeds + (size_t)th * 4) = make_uint4(g.x, g.y, g.z, g.w);
+        if (t == 0) *(uint4 *)(sd.wseeds + (size_t)w * 4) = make_uint4(ws.x, ws.y, ws.z, ws.w);
+#pragma unroll
+        for (int k = 0; k < Sys::NOPS; k++) atomicAdd(s_op + wl * Sys::NOPS + k, opd[k]);
+    }
+    __syncthreads();
+    {
+        const size_t base = (size_t)w0 * DOF * N;
+        const int count = n_here * DOF * N;
+        for (int i = tid; i < count; i += blockDim.x) {
+            const int wi = i / (DOF * N), r = i - wi * (DOF * N);
+            const int d = r / N, sl = r - d * N;
+            sd.paths[base + i] = FSB_AT(smem + wi * wstride, d, sl);
+        }
+        for (int i = tid; i < n_here * sd.nops; i += blockDim.x) sd.op_sums[(size_t)w0 * sd.nops + i] += s_op[i];
+    }
+    __syncthreads();  // the next tile reuses the shared-memory tile
+#undef FSB_AT
+}

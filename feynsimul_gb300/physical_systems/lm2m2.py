@@ -253,6 +253,11 @@ inline FLOAT_TYPE lm2m2_cluster_pair_r2_sum({args})
             np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
             np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1)], 1)
         r0 = np.einsum("wij,nj->wni", R, base) * L[:, None, None]  # [walkers, n, 3]
-        r = r0[:, None, :, :] + rng.normal(0.0, noise, size=(walkers, N, n, 3))
-        xi = self.positions_to_jacobi(r)  # [walkers, N, DOF]
-        return np.ascontiguousarray(np.transpose(xi, (0, 2, 1)).reshape(walkers, self.DOF * N))
+        xi0 = self.positions_to_jacobi(r0)                        # [walkers, DOF]
+        paths = np.repeat(xi0[:, :, None], N, axis=2)              # [walkers, DOF, N]
+        if noise > 0:
+            # isotropic Cartesian noise of width `noise` is isotropic noise of width
+            # noise*sqrt(m) in mass-scaled Jacobi coordinates (the transformation is
+            # sqrt(m) times an orthogonal one for equal masses)
+            paths = paths + rng.normal(0.0, noise * np.sqrt(self.m), size=paths.shape)
+        return np.ascontiguousarray(paths.reshape(walkers, self.DOF * N))

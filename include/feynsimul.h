@@ -234,6 +234,42 @@ int fs_mlp_infer(const void *frag, const float *bias, const float *x, float *y, 
 int fs_set_learned_proposal(fs_handle *h, const void *frag, size_t frag_bytes, const float *bias,
                             size_t n_bias, double inv_scale);
 
+/* ---- ragged batch (no counterpart in the reference) ----
+ * Many independent systems in one persistent launch: each system has its own plugin
+ * type (potential and operators compiled once per type), slice count, bisection level,
+ * beta and walker count.  Work items are tiles of walkers; CTAs take them from a work
+ * counter, largest first.  Sampling semantics are those of the fixed-mode xorshift sweep
+ * (per-thread float streams, per-walker offset streams), FP32 paths, FP64 operator sums
+ * per walker accumulated over launches. */
+typedef struct fs_batch fs_batch;
+typedef struct fs_batch_system {
+    int32_t type;              /* index into the per-type plugin arrays */
+    int32_t n_walkers;
+    int32_t n_slices;          /* N, a power of two */
+    int32_t bisection_level;   /* S, 1..10; N / 2^S threads per walker */
+    double beta;
+    int32_t walkers_per_tile;  /* 0 = as many as fit the block (output: the value used) */
+} fs_batch_system;
+int fs_batch_create(int32_t n_types, const int32_t *type_dof, const char *const *potentials,
+                    const char *const *user_codes, const char *const *operators, int32_t n_ops,
+                    int32_t n_systems, const fs_batch_system *systems, int32_t op_runs,
+                    int32_t msteps, int32_t block_threads, fs_batch **out);
+int fs_batch_destroy(fs_batch *b);
+/* n_launches persistent launches; use_graph = 1 replays a captured CUDA graph (counter
+ * reset + launch) instead of launching directly.  Asynchronous. */
+int fs_batch_run(fs_batch *b, int32_t n_launches, int32_t use_graph);
+int fs_batch_sync(fs_batch *b);
+int fs_batch_get_run_time(fs_batch *b, double *seconds);
+int fs_batch_set_paths(fs_batch *b, int32_t system, const float *host, size_t n);
+int fs_batch_get_paths(fs_batch *b, int32_t system, float *host, size_t n);
+int fs_batch_set_seeds(fs_batch *b, int32_t system, const uint32_t *thread_rows, size_t n_threads,
+                       const uint32_t *walker_rows, size_t n_walkers);
+int fs_batch_get_op_sums(fs_batch *b, int32_t system, double *out, size_t n);
+int fs_batch_get_accepts(fs_batch *b, int32_t system, uint32_t *out, size_t n);
+int fs_batch_query(const fs_batch *b, int64_t *node_updates_per_launch, int64_t *smem_bytes,
+                   int64_t *registers, int64_t *n_items, int64_t *grid, int64_t *walkers_per_tile,
+                   size_t n_systems);
+
 /* Library version string. */
 const char *fs_version(void);
 

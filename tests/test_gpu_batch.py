@@ -1,0 +1,68 @@
+"""Ragged batch on the GPU: every system of a batch evolves exactly as the single-system
+sweep with the same seeds and paths (fixed-mode xorshift, fast math, FP64 sums)."""
+import numpy as np
+import pytest
+
+from gpu_util import engine, require_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_matches_single_system_kernels():
+    require_gpu()
+    kernel, kernel_args = engine()
+    from feynsimul_gb300.batch import BatchSampler
+    from feynsimul_gb300.physical_systems.lm2m2 import Lm2m2Cluster
+    workload = [{"n": 3, "N": 64, "T": 1.0, "walkers": 96}, {"n": 4, "N": 128, "T": 0.7, "walkers": 64},
+                {"n": 3, "N": 256, "T": 1.7, "walkers": 32}, {"n": 5, "N": 64, "T": 1.2, "walkers": 64}]
+    op_runs, msteps = 2, 3
+    b = BatchSampler(workload, op_runs=op_runs, msteps=msteps, block_threads=256, tpw_target=16)
+    rng = np.random.RandomState(5)
+    singles = []
+    for i, w in enumerate(workload):
+        c = Lm2m2Cluster(w["n"], w["T"])
+        S = b.systems[i].bisection_level
+        tpw = w["N"] >> S
+        paths = c.initial_paths(w["walkers"], w["N"], rng).astype(np.float32)
+        ts = rng.randint(0, 2 ** 31 - 1, size=(w["walkers"] * tpw + 1, 4)).astype(np.uint32)
+        ws = rng.randint(0, 2 ** 31 - 1, size=(w["walkers"], 4)).astype(np.uint32)
+        b.set_state(i, paths, ts[:-1], ws)
+        ka = kernel_args.KernelArgs(
+            system=c, nbrOfWalkers=w["walkers"], N=w["N"], beta=float(1.0 / w["T"]), S=S, enableOperator=True,
+            enableCorrelator=False, enableBisection=True, enablePathShift=False, enableSingleNodeMove=False,
+            enableBins=False, nbrOfWalkersPerWorkGroup=1, enableParallelizePath=True, enableGlobalPath=False,
+            enableGlobalOldPath=False, operators=(c.energyOp,), operatorRuns=op_runs,
+            metroStepsPerOperatorRun=msteps, fastMath=True, accumulation="fp64")
+        k = kernel.PIMCKernel(ka)
+        k.setPaths(paths)
+        k.setSeeds(ts)
+        k.setWalkerSeeds(ws)
+        singles.append(k)
+    b.run(1, graph=True)
+    for i, (w, k) in enumerate(zip(workload, singles)):
+        k.run()
+        acc_b, acc_s = b.accepts(i), k.getAccepts()
+        same = np.all(np.isclose(b.paths(i), k.getPaths(), rtol=1e-4, atol=1e-4), axis=1)
+        assert same.mean() > 0.95, (i, same.mean())
+        assert (acc_b != acc_s).sum() <= max(2, acc_s.size // 100), i
+        # per-walker energy: batch keeps sums over (runs x slices), the kernel per-walker means
+        e_b = b.energy_sums(i) / (op_runs * w["N"])
+        e_s = k.getOperators()[0]
+        np.testing.assert_allclose(e_b[same], e_s[same], rtol=1e-3, atol=1e-3)
+        k.close()
+    # a second launch through the captured graph continues the same chains
+    t = b.run(2, graph=True)
+    assert t > 0
+    b.close()
+
+
+def test_autotune_caches(tmp_path):
+    require_gpu()
+    engine()
+    from feynsimul_gb300.batch import autotune, ragged_workload
+    wl = ragged_workload(seed=3, n_systems=6, walker_range=(64, 256))
+    cache = str(tmp_path / "tune.json")
+    r1 = autotune(wl, candidates=[(256, 16), (128, 16)], cache_file=cache, launches=1)
+    assert not r1["cached"] and r1["node_updates_per_s"] > 0
+    r2 = autotune(wl, candidates=[(256, 16), (128, 16)], cache_file=cache, launches=1)
+    assert r2["cached"] and r2["block_threads"] == r1["block_threads"]
