@@ -327,6 +327,26 @@ def batch_bench(args):
 
 
 # ------------------------------------------------------------------ arms
+def precision_bench(args):
+    """The precision study on the 10-atom LM2M2 cluster, N = 1024, 2^20 walkers (FP32 path,
+    FP64 / plain-FP32 / Kahan sums) against 2^14 walkers run FP64 everywhere from the same
+    seeds (feynsimul_gb300.precision)."""
+    from feynsimul_gb300.precision import precision_study
+    kw = {}
+    if args.walkers:
+        kw["walkers"] = args.walkers
+        kw["fp64_walkers"] = min(2 ** 14, args.walkers)
+    if args.op_runs:
+        kw["op_runs"] = args.op_runs
+    if args.msteps:
+        kw["msteps"] = args.msteps
+    r = precision_study(launches=max(2, args.steps), log=lambda m: print(m, file=sys.stderr), **kw)
+    return {"metric": "precision study: FP32-path error vs FP64-everywhere, per result",
+            "value": r["fp32_node_updates_per_s"], "unit": "node-updates/s (FP32 path, study sums)",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "f32 path, f64/f32/kahan sums",
+            "data": "synthetic, seeded", "config": {"workload": r["workload"]}, "study": r}
+
+
 def run_gb300(args, rank, world):
     from feynsimul_gb300 import build as fb
     fb.build()
@@ -441,7 +461,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="he3", choices=["he3", "ho", "learned", "batch"])
+    ap.add_argument("--config", default="he3", choices=["he3", "ho", "learned", "batch", "precision"])
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain ESS study")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -487,6 +507,10 @@ def main():
     if args.config == "learned":
         if rank == 0:
             print(json.dumps(learned_study(quick=False)))
+        return
+    if args.config == "precision":
+        if rank == 0:
+            print(json.dumps(precision_bench(args)))
         return
     if world > 1:
         import torch

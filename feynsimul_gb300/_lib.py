@@ -36,6 +36,7 @@ EXPORTS = (
     "fs_mlp_pack", "fs_mlp_infer", "fs_set_learned_proposal", "fs_batch_create", "fs_batch_destroy",
     "fs_batch_run", "fs_batch_sync", "fs_batch_get_run_time", "fs_batch_set_paths", "fs_batch_get_paths",
     "fs_batch_set_seeds", "fs_batch_get_op_sums", "fs_batch_get_accepts", "fs_batch_query",
+    "fs_reduce_correlator", "fs_set_paths_tiled",
 )
 
 
@@ -52,7 +53,7 @@ class FsConfig(ctypes.Structure):
         ("hist_lo", ctypes.c_double), ("hist_hi", ctypes.c_double), ("hist_bins", ctypes.c_int32),
         ("compat", ctypes.c_int32), ("accum", ctypes.c_int32), ("fast_math", ctypes.c_int32),
         ("walkers_per_block", ctypes.c_int32), ("min_blocks_per_sm", ctypes.c_int32),
-        ("learned", ctypes.c_int32),
+        ("learned", ctypes.c_int32), ("global_path", ctypes.c_int32),
     ]
 
 
@@ -107,6 +108,8 @@ _PROTOS = {
     "fs_sync_timeout": ([_P, ctypes.c_double], ctypes.c_int),
     "fs_get_operators": ([_P, _P, _S], ctypes.c_int),
     "fs_get_correlator": ([_P, _P, _S], ctypes.c_int),
+    "fs_reduce_correlator": ([_P, ctypes.c_int64, ctypes.c_int64, _P, _P, _S], ctypes.c_int),
+    "fs_set_paths_tiled": ([_P, _P, _S], ctypes.c_int),
     "fs_get_accepts": ([_P, _P, _S], ctypes.c_int),
     "fs_get_bins": ([_P, _P, _S], ctypes.c_int),
     "fs_get_histogram": ([_P, _P, _S], ctypes.c_int),

@@ -52,6 +52,13 @@ __attribute__((visibility("hidden"))) const char *fsi_batch_src() { return kBatc
 // ------------------------------------------------------------------ errors
 static thread_local std::string g_thread_err;
 
+// host image of the device's precision-study correlator accumulator (fs_pimc.cuh FsCorAcc)
+struct FsCorStudyHost {
+    double d;
+    float f, ks, kc, pad;
+};
+static_assert(sizeof(FsCorStudyHost) == 24, "study accumulator layout");
+
 struct fs_handle {
     fs_config cfg{};
     int device = 0;
@@ -64,7 +71,8 @@ struct fs_handle {
     size_t smem = 0;
     int regs = 0;
     size_t ft = 4, op_elem = 8, cor_elem = 8;
-    size_t n_ops_elems = 0, n_cor_elems = 0, n_bins = 0, n_hist = 0;
+    size_t n_ops_elems = 0, n_cor_elems = 0, n_cor_lags = 0, n_bins = 0, n_hist = 0;
+    double *d_red = nullptr;  // fs_reduce_correlator output (sum, sumsq)
     // CUDA objects
     cudaLibrary_t lib = nullptr;
     cudaKernel_t k_metro = nullptr, k_rinit = nullptr;
@@ -300,7 +308,8 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << "\n#define FS_MSTEPS " << c.metro_steps_per_operator_run << "\n#define FS_EPS "
       << lit(c.beta / (double)c.n_slices) << "\n#define FS_OPNORM " << lit(opnorm)
       << "\n#define FS_BINS " << (c.enable_bins ? 1 : 0) << "\n#define FS_NHIST " << nhist
-      << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n";
+      << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n#define FS_GLOBAL " << (c.global_path ? 1 : 0)
+      << "\n";
     {
         char b[64];
         snprintf(b, sizeof b, "%.9E", (double)(c.ranlux_int_max + 1ull));
@@ -526,7 +535,7 @@ static void free_buffers(fs_handle *h)
 {
     void *bufs[] = {h->d_paths, h->d_accepts, h->d_seeds, h->d_snap, h->d_wseeds, h->d_rtab,
                     h->d_gtab, h->d_bins, h->d_ops, h->d_cor, h->d_hist, h->d_status,
-                    h->d_mlp_frag, h->d_mlp_bias};
+                    h->d_mlp_frag, h->d_mlp_bias, h->d_red};
     for (void *p : bufs)
         if (p) cudaFree(p);
 }
@@ -575,8 +584,10 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     long long wstride = (long long)c.dof * dstride;
     wstride = ((wstride + 15) / 16) * 16;
     if ((wstride / 16) % 2 == 0) wstride += 16;
+    if (c.global_path) wstride = (long long)c.dof * c.n_slices;  // no shared-memory path
     h->wstride = wstride;
-    const size_t per_walker = (size_t)(wstride + (long long)h->cors.size() * c.n_slices) * h->ft;
+    const size_t per_walker =
+        (size_t)((c.global_path ? 0 : wstride) + (long long)h->cors.size() * c.n_slices) * h->ft;
     const size_t hist_bytes = (size_t)(c.hist_bins > 0 && !h->hists.empty() ? c.hist_bins : 0) * 4;
     if (c.walkers_per_block > 0) {
         h->wpb = c.walkers_per_block;
@@ -714,12 +725,13 @@ extern "C" int fs_create(const fs_config *cfg, const char *potential, const char
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) cudaGetLastError();
     h->op_elem = c.accum == 0 ? h->ft : (c.accum == 2 ? 4 : 8);
     h->n_ops_elems = T * h->ops.size() * (c.accum == 3 ? 3 : 1);
-    h->cor_elem = c.accum == 0 ? h->ft : 8;
-    h->n_cor_elems = W * h->cors.size() * (N / 2);
+    h->cor_elem = c.accum == 0 ? h->ft : (c.accum == 3 ? 24 : 8);
+    h->n_cor_lags = W * h->cors.size() * (N / 2);
+    h->n_cor_elems = h->n_cor_lags * (c.accum == 3 ? 4 : 1);
     h->n_bins = c.enable_bins ? (size_t)std::llround(std::pow((double)c.bin_resolution_per_dof, c.dof)) : 0;
     h->n_hist = h->hists.empty() ? 0 : (size_t)c.hist_bins;
     h->g_rows = c.compat ? T : W;
-    size_t need = W * c.dof * N * h->ft + T * 4 + h->n_ops_elems * h->op_elem + h->n_cor_elems * h->cor_elem +
+    size_t need = W * c.dof * N * h->ft + T * 4 + h->n_ops_elems * h->op_elem + h->n_cor_lags * h->cor_elem +
                   h->n_bins * 4 + h->n_hist * 8 +
                   (c.enable_ranlux ? (T + h->g_rows) * 112 : ((T + 1) * 16 * 2 + W * 16));
     if (free_b && need > free_b) {
@@ -741,7 +753,7 @@ extern "C" int fs_create(const fs_config *cfg, const char *potential, const char
         CREATE_TRY(dalloc(h, (void **)&h->d_wseeds, W * 16));
     }
     CREATE_TRY(dalloc(h, &h->d_ops, h->n_ops_elems * h->op_elem));
-    CREATE_TRY(dalloc(h, &h->d_cor, h->n_cor_elems * h->cor_elem));
+    CREATE_TRY(dalloc(h, &h->d_cor, h->n_cor_lags * h->cor_elem));
     CREATE_TRY(dalloc(h, (void **)&h->d_bins, h->n_bins * 4));
     CREATE_TRY(dalloc(h, (void **)&h->d_hist, h->n_hist * 8));
     CREATE_TRY(dalloc(h, (void **)&h->d_status, 16));
@@ -1014,11 +1026,24 @@ extern "C" int fs_get_correlator(fs_handle *h, double *out, size_t n)
 {
     if (!h) return FS_ERR_CONFIG;
     if (n != h->n_cor_elems) return fail(h, FS_ERR_IO, "expected %zu correlator values", h->n_cor_elems);
-    std::vector<unsigned char> raw(n * h->cor_elem + 1);
-    int rc = copy_out(h, raw.data(), h->d_cor, n * h->cor_elem, n * h->cor_elem);
+    const size_t bytes = h->n_cor_lags * h->cor_elem;
+    std::vector<unsigned char> raw(bytes + 1);
+    int rc = copy_out(h, raw.data(), h->d_cor, bytes, bytes);
     if (rc) return rc;
-    if (h->cor_elem == 4) widen<float>(raw, out, n);
-    else widen<double>(raw, out, n);
+    if (h->cor_elem == 24) {
+        for (size_t i = 0; i < h->n_cor_lags; i++) {
+            FsCorStudyHost v;
+            memcpy(&v, raw.data() + i * 24, 24);
+            out[4 * i + 0] = v.f;
+            out[4 * i + 1] = v.ks;
+            out[4 * i + 2] = v.kc;
+            out[4 * i + 3] = v.d;
+        }
+    } else if (h->cor_elem == 4) {
+        widen<float>(raw, out, n);
+    } else {
+        widen<double>(raw, out, n);
+    }
     return FS_OK;
 }
 
@@ -1050,7 +1075,112 @@ extern "C" int fs_set_correlator(fs_handle *h, const double *in, size_t n)
     if (!h) return FS_ERR_CONFIG;
     if (n != h->n_cor_elems) return fail(h, FS_ERR_IO, "expected %zu correlator values", h->n_cor_elems);
     if (n == 0) return FS_OK;
+    if (h->cor_elem == 24) {
+        std::vector<FsCorStudyHost> tmp(h->n_cor_lags + 1);
+        for (size_t i = 0; i < h->n_cor_lags; i++)
+            tmp[i] = FsCorStudyHost{in[4 * i + 3], (float)in[4 * i + 0], (float)in[4 * i + 1], (float)in[4 * i + 2], 0.f};
+        return copy_in(h, h->d_cor, tmp.data(), h->n_cor_lags * 24, h->n_cor_lags * 24);
+    }
     return h->cor_elem == 4 ? set_widened<float>(h, h->d_cor, in, n) : set_widened<double>(h, h->d_cor, in, n);
+}
+
+// ---- correlator moments over a walker range, on the device ----
+// Block b reduces walkers [w0 + b*chunk, ...) for every lag (threads stride the lags, so
+// a warp reads consecutive lags of one walker) and adds its partial sums atomically.
+template <int KIND>  // 0: float, 1: double, 2: study struct (3 columns)
+__global__ void fs_cor_moments_kernel(const unsigned char *cor, size_t lags, long long w0, long long w1,
+                                      long long chunk, double *sum, double *sq)
+{
+    constexpr int NC = KIND == 2 ? 3 : 1;
+    const long long wb = w0 + (long long)blockIdx.x * chunk;
+    const long long we = wb + chunk < w1 ? wb + chunk : w1;
+    for (size_t l = threadIdx.x; l < lags; l += blockDim.x) {
+        double s[NC], q[NC];
+#pragma unroll
+        for (int k = 0; k < NC; k++) s[k] = q[k] = 0.0;
+        for (long long w = wb; w < we; w++) {
+            const size_t i = (size_t)w * lags + l;
+            double v[NC];
+            if (KIND == 0) {
+                v[0] = (double)((const float *)cor)[i];
+            } else if (KIND == 1) {
+                v[0] = ((const double *)cor)[i];
+            } else {
+                const unsigned char *e = cor + i * 24;
+                v[0] = (double)*(const float *)(e + 8);
+                v[NC > 1 ? 1 : 0] = (double)*(const float *)(e + 12);
+                v[NC > 2 ? 2 : 0] = *(const double *)e;
+            }
+#pragma unroll
+            for (int k = 0; k < NC; k++) {
+                s[k] += v[k];
+                q[k] += v[k] * v[k];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NC; k++) {
+            atomicAdd(sum + l * NC + k, s[k]);
+            atomicAdd(sq + l * NC + k, q[k]);
+        }
+    }
+}
+
+extern "C" int fs_reduce_correlator(fs_handle *h, int64_t walker_begin, int64_t walker_end, double *sum,
+                                    double *sumsq, size_t n)
+{
+    if (!h || !sum || !sumsq) return FS_ERR_CONFIG;
+    const size_t W = (size_t)h->cfg.n_walkers;
+    const size_t lags = h->cors.size() * (size_t)(h->cfg.n_slices / 2);
+    const int ncol = h->cor_elem == 24 ? 3 : 1;
+    if (lags == 0) return fail(h, FS_ERR_STATE, "no correlators");
+    if (n != lags * ncol) return fail(h, FS_ERR_IO, "expected %zu values", lags * ncol);
+    if (walker_begin < 0 || walker_end > (int64_t)W || walker_begin >= walker_end)
+        return fail(h, FS_ERR_IO, "walker range [%lld, %lld) outside [0, %zu)", (long long)walker_begin,
+                    (long long)walker_end, W);
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    if (!h->d_red) CUDA_TRY(h, cudaMalloc((void **)&h->d_red, 2 * lags * 3 * sizeof(double)), FS_ERR_OOM);
+    CUDA_TRY(h, cudaMemsetAsync(h->d_red, 0, 2 * n * sizeof(double), h->stream), FS_ERR_CUDA);
+    const long long nw = walker_end - walker_begin;
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    const long long blocks = std::min<long long>(nw, (long long)sms * 8);
+    const long long chunk = (nw + blocks - 1) / blocks;
+    const unsigned grid = (unsigned)((nw + chunk - 1) / chunk);
+    const unsigned char *c = (const unsigned char *)h->d_cor;
+    double *s = h->d_red, *q = h->d_red + n;
+    if (h->cor_elem == 24)
+        fs_cor_moments_kernel<2><<<grid, 256, 0, h->stream>>>(c, lags, walker_begin, walker_end, chunk, s, q);
+    else if (h->cor_elem == 8)
+        fs_cor_moments_kernel<1><<<grid, 256, 0, h->stream>>>(c, lags, walker_begin, walker_end, chunk, s, q);
+    else
+        fs_cor_moments_kernel<0><<<grid, 256, 0, h->stream>>>(c, lags, walker_begin, walker_end, chunk, s, q);
+    CUDA_TRY(h, cudaGetLastError(), FS_ERR_LAUNCH);
+    CUDA_TRY(h, cudaMemcpyAsync(sum, s, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaMemcpyAsync(sumsq, q, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
+    return FS_OK;
+}
+
+extern "C" int fs_set_paths_tiled(fs_handle *h, const void *host, size_t n_template)
+{
+    if (!h || !host) return FS_ERR_CONFIG;
+    const size_t W = (size_t)h->cfg.n_walkers;
+    if (n_template == 0 || n_template > W)
+        return fail(h, FS_ERR_IO, "template walker count %zu outside [1, %zu]", n_template, W);
+    const size_t wb = (size_t)h->cfg.dof * h->cfg.n_slices * h->ft;
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_paths, host, n_template * wb, cudaMemcpyHostToDevice, h->stream), FS_ERR_CUDA);
+    // doubling copies: walkers [0, k) -> [k, 2k) keep w % n_template because k is a
+    // multiple of n_template
+    size_t k = n_template;
+    while (k < W) {
+        const size_t m = std::min(k, W - k);
+        CUDA_TRY(h, cudaMemcpyAsync((char *)h->d_paths + k * wb, h->d_paths, m * wb, cudaMemcpyDeviceToDevice,
+                                    h->stream), FS_ERR_CUDA);
+        k += m;
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
+    return FS_OK;
 }
 extern "C" int fs_set_bins(fs_handle *h, const uint32_t *in, size_t n)
 {
@@ -1067,7 +1197,7 @@ extern "C" int fs_zero_accumulators(fs_handle *h)
 {
     if (!h) return FS_ERR_CONFIG;
     CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
-    if (h->n_cor_elems) CUDA_TRY(h, cudaMemsetAsync(h->d_cor, 0, h->n_cor_elems * h->cor_elem, h->stream), FS_ERR_CUDA);
+    if (h->n_cor_lags) CUDA_TRY(h, cudaMemsetAsync(h->d_cor, 0, h->n_cor_lags * h->cor_elem, h->stream), FS_ERR_CUDA);
     if (h->n_bins) CUDA_TRY(h, cudaMemsetAsync(h->d_bins, 0, h->n_bins * 4, h->stream), FS_ERR_CUDA);
     if (h->n_hist) CUDA_TRY(h, cudaMemsetAsync(h->d_hist, 0, h->n_hist * 8, h->stream), FS_ERR_CUDA);
     CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);

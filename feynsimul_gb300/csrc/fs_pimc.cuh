@@ -25,15 +25,24 @@
 #define FS_THREADS (FS_NWALKERS * FS_TPW)
 #define FS_BLOCK (FS_WPB * FS_TPW)
 #define FS_LPT ((FS_HALF_N + FS_TPW - 1) / FS_TPW)  // correlator lags owned per thread
-#define FS_COR_REGS (FS_LPT * FS_NCOR <= 16)
+#define FS_COR_REGS (FS_ACCUM != 3 && FS_LPT * FS_NCOR <= 16)
 
 // Shared-memory path layout.  Slice s of degree d of a walker sits at d * FS_DSTRIDE +
 // FS_PHYS(s) with one padding word after every 2^S slices: the segment threads of a walker
 // read slices 2^S apart, which the padding turns into 2^S + 1 words apart, an odd stride,
 // so the threads of a warp hit distinct banks.  FS_WSTRIDE (walker stride, from the host)
 // is an odd multiple of 16 words so two walkers sharing a warp use opposite bank halves.
+//
+// Global-path mode (FS_GLOBAL, the reference's ENABLE_GLOBAL_PATH, kernel.c:62-70 and
+// :582-588): the walker's threads work in place on its [DOF][N] rows of the paths array
+// (cached in L1/L2), for paths larger than shared memory; same arithmetic, same results.
+#if FS_GLOBAL
+#define FS_PHYS(s) (s)
+#define FS_DSTRIDE FS_N
+#else
 #define FS_PHYS(s) ((s) + ((s) >> FS_S))
 #define FS_DSTRIDE (FS_N + (FS_N >> FS_S))
+#endif
 #define FS_AT(P, d, s) (P)[(d) * FS_DSTRIDE + FS_PHYS(s)]
 
 #if FS_DOUBLE
@@ -110,7 +119,10 @@ __device__ __forceinline__ fs_u32 fs_offset(FsIStream &g, fs_u32 range)
 #define FS_OLD_N 1
 #endif
 
-#if FS_RANLUX
+// Rolled move loops for RANLUX (its generator calls are large) and for big plugins (a
+// fully unrolled move repeats the potential 2 * (2^S - 1) times, which for a 10-atom
+// cluster costs minutes of compilation and overflows the instruction cache)
+#if FS_RANLUX || FS_DOF > 8
 #define FS_MOVE_UNROLL _Pragma("unroll 1")
 #else
 #define FS_MOVE_UNROLL _Pragma("unroll")
@@ -244,6 +256,12 @@ __device__ __forceinline__ int fs_thread_id(int w, int t)
 
 #if FS_ACCUM == 0
 typedef FT FsCorAcc;
+#elif FS_ACCUM == 3
+// precision study: the same products summed in plain FP32, Kahan FP32 and FP64 (24 bytes)
+struct FsCorAcc {
+    double d;
+    float f, ks, kc, pad;
+};
 #else
 typedef double FsCorAcc;
 #endif
@@ -269,8 +287,12 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     __shared__ FsIStream s_istream[FS_WPB];
     __shared__ fs_u32 s_off[FS_WPB];
 #endif
+#if FS_GLOBAL
+    FT *s_cor = (FT *)fs_smem;                                   // [WPB][NCOR][N]
+#else
     FT *s_path = (FT *)fs_smem;                                  // [WPB][DOF*N]
     FT *s_cor = s_path + FS_WPB * FS_WSTRIDE;                    // [WPB][NCOR][N]
+#endif
     fs_u32 *s_hist = (fs_u32 *)(s_cor + FS_WPB * FS_NCOR * FS_N);  // [HBINS]
 
     const int tid_b = threadIdx.x;
@@ -283,6 +305,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 
     // ---- path in (coalesced global reads; padded shared layout) ----
     {
+#if !FS_GLOBAL
         const size_t base = (size_t)w0 * FS_DOF * FS_N;
         const int count = n_here * FS_DOF * FS_N;
         for (int i = tid_b; i < count; i += FS_BLOCK) {
@@ -290,6 +313,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             const int d = r / FS_N, sl = r - d * FS_N;
             FS_AT(s_path + wi * FS_WSTRIDE, d, sl) = a.paths[base + i];
         }
+#endif
 #if FS_NHIST > 0
         for (int i = tid_b; i < FS_HBINS; i += FS_BLOCK) s_hist[i] = 0u;
 #endif
@@ -305,7 +329,11 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #else
 #define FS_WSYNC() __syncthreads()
 #endif
+#if FS_GLOBAL
+        FT *P = a.paths + (size_t)w * FS_DOF * FS_N;
+#else
         FT *P = s_path + wl * FS_WSTRIDE;
+#endif
         const int tid = fs_thread_id(w, t);
         // sigma table (kernel.c:608-618), computed on the host with the same FP operations
         const FT *sigma = fs_sigma;
@@ -519,6 +547,11 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                     for (int s1 = 0; s1 < FS_N; s1++) {
 #if FS_ACCUM == 0
                         acc = FS_ADD(acc, FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]));
+#elif FS_ACCUM == 3
+                        const FT pr = FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]);
+                        acc.f = __fadd_rn(acc.f, (float)pr);
+                        fs_kahan(acc.ks, acc.kc, (float)pr);
+                        acc.d = __dadd_rn(acc.d, (double)pr);
 #else
                         acc = __dadd_rn(acc, (double)FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]));
 #endif
@@ -583,6 +616,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 
     // ---- path out (coalesced global writes) ----
     {
+#if !FS_GLOBAL
         const size_t base = (size_t)w0 * FS_DOF * FS_N;
         const int count = n_here * FS_DOF * FS_N;
         for (int i = tid_b; i < count; i += FS_BLOCK) {
@@ -590,6 +624,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             const int d = r / FS_N, sl = r - d * FS_N;
             a.paths[base + i] = FS_AT(s_path + wi * FS_WSTRIDE, d, sl);
         }
+#endif
 #if FS_NHIST > 0
         for (int i = tid_b; i < FS_HBINS; i += FS_BLOCK)
             if (s_hist[i]) atomicAdd(a.hist + i, (fs_u64)s_hist[i]);

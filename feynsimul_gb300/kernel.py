@@ -194,6 +194,9 @@ class PIMCKernel:
         c.walkers_per_block = self._walkersPerBlock
         c.min_blocks_per_sm = int(getattr(ka, "minBlocksPerSM", 0) or 0)
         c.learned = int(bool(getattr(ka, "learnedProposal", False)))
+        # enableGlobalOldPath (kernel.c:259-276) has no counterpart: the saved old segment
+        # is per-thread private data either way (registers, spilling to local memory)
+        c.global_path = int(bool(self._enableGlobalPath)) if self._enableBisection else 0
         self._learned = bool(c.learned)
         self._cfg = c
 
@@ -321,6 +324,15 @@ class PIMCKernel:
         check(lib().fs_get_paths(self._handle, out.ctypes.data, out.size), self._handle)
         return out
 
+    def setPathsTiled(self, template):
+        """Fill every walker's path from a few template walkers (shape (k, N * DOF)):
+        walker w gets template w % k, replicated on the device."""
+        a = np.ascontiguousarray(np.asarray(template), dtype=self._ftype)
+        per = self._N * self._system.DOF
+        if a.size % per or a.size == 0:
+            raise ValueError("template must hold whole walkers of N * DOF elements")
+        check(lib().fs_set_paths_tiled(self._handle, a.ctypes.data, a.size // per), self._handle)
+
     def setPaths(self, paths):
         """Set the paths (kernel.py:567-574)."""
         a = np.ascontiguousarray(np.asarray(paths), dtype=self._ftype)
@@ -383,15 +395,59 @@ class PIMCKernel:
         if not self._enableCorrelator:
             raise Exception("Can only return correlator when created with"
                             "kernalArg.enableCorrelator = True")
-        n = self._nbrOfWalkers * len(self._correlators) * (self._N // 2)
-        raw = np.empty(n, np.float64)
-        check(lib().fs_get_correlator(self._handle, raw.ctypes.data, n), self._handle)
+        raw = self._raw_correlator()
+        if self._accumulation == "study":
+            raw = raw.reshape(-1, 4)[:, 3]
         vals = raw.reshape(self._nbrOfWalkers, len(self._correlators), self._N // 2)
         runs = 1 if self._compat else max(1, self._runsSinceZero)
         vals = vals / float(runs)
         mean = vals.mean(axis=0) / float(self._operatorRuns * self._N)
         se = vals.std(axis=0) / np.sqrt(self._nbrOfWalkers)
         return (mean, se)
+
+    def _cor_count(self):
+        return self._nbrOfWalkers * len(self._correlators) * (self._N // 2) * \
+            (4 if self._accumulation == "study" else 1)
+
+    def _raw_correlator(self):
+        n = self._cor_count()
+        raw = np.empty(n, np.float64)
+        check(lib().fs_get_correlator(self._handle, raw.ctypes.data, n), self._handle)
+        return raw
+
+    def _cor_norm(self):
+        runs = 1 if self._compat else max(1, self._runsSinceZero)
+        return 1.0 / (float(runs) * self._operatorRuns * self._N)
+
+    def getCorrelatorStudy(self):
+        """Precision study: per-walker correlator means (3, walkers, nCorr, N/2) from the plain
+        FP32, Kahan-FP32 and FP64 sums of the same products."""
+        if self._accumulation != "study":
+            raise Exception("create the kernel with accumulation='study'")
+        raw = self._raw_correlator().reshape(self._nbrOfWalkers, len(self._correlators), self._N // 2, 4)
+        return np.stack([raw[..., 0], raw[..., 1], raw[..., 3]]) * self._cor_norm()
+
+    def getCorrelatorMoments(self, walkers=None):
+        """Correlator mean and standard error over a walker range (default all), reduced on
+        the device: (mean, se), each (nCorr, N/2), or (3, nCorr, N/2) in "study"
+        accumulation (plain FP32, Kahan, FP64 sums)."""
+        if not self._enableCorrelator:
+            raise Exception("Can only return correlator when created with"
+                            "kernalArg.enableCorrelator = True")
+        w0, w1 = walkers if walkers is not None else (0, self._nbrOfWalkers)
+        ncol = 3 if self._accumulation == "study" else 1
+        n = len(self._correlators) * (self._N // 2) * ncol
+        s, q = np.empty(n, np.float64), np.empty(n, np.float64)
+        check(lib().fs_reduce_correlator(self._handle, int(w0), int(w1), s.ctypes.data, q.ctypes.data, n),
+              self._handle)
+        nw = float(w1 - w0)
+        f = self._cor_norm()
+        mean = s / nw
+        var = np.maximum(q / nw - mean * mean, 0.0)
+        shape = (len(self._correlators), self._N // 2, ncol)
+        mean = np.moveaxis((mean * f).reshape(shape), -1, 0)
+        se = np.moveaxis((np.sqrt(var / nw) * f).reshape(shape), -1, 0)
+        return (mean[0], se[0]) if ncol == 1 else (mean, se)
 
     def zeroAccumulators(self):
         """Reset correlator sums, bins and histogram counts."""
@@ -523,10 +579,7 @@ class PIMCKernel:
             if not self._compat:
                 st["walker_seeds"] = self.getWalkerSeeds()
         if self._enableCorrelator:
-            n = self._nbrOfWalkers * len(self._correlators) * (self._N // 2)
-            cor = np.empty(n, np.float64)
-            check(L.fs_get_correlator(self._handle, cor.ctypes.data, n), self._handle)
-            st["correlator"] = cor
+            st["correlator"] = self._raw_correlator()
         if self._enableBins:
             st["bins"] = self.getBinCountsRaw()
         if self._histBins:

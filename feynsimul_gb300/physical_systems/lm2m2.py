@@ -235,15 +235,21 @@ inline FLOAT_TYPE lm2m2_cluster_pair_r2_sum({args})
 
     def initial_paths(self, walkers: int, N: int, rng, side=(3.0, 5.0), noise=0.1):
         """Paths [walkers, DOF*N] (DOF-major): for n = 3 a random equilateral triangle of
-        side U(side) with random orientation, otherwise random points on a sphere with the
-        same nearest-neighbour scale; plus N(0, noise) Angstrom per slice and coordinate."""
+        side U(side) with random orientation, otherwise n quasi-uniform points on a sphere
+        (Fibonacci lattice) whose closest pair is U(side) apart, randomly oriented; plus
+        N(0, noise) Angstrom per slice and coordinate."""
         n = self.n
         L = rng.uniform(side[0], side[1], size=walkers)
         if n == 3:
             base = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.5, np.sqrt(3) / 2, 0.0]])
         else:
-            g = rng.standard_normal((n, 3))
-            base = g / np.linalg.norm(g, axis=1, keepdims=True) * (0.5 * np.sqrt(n))
+            k = np.arange(n) + 0.5
+            z = 1.0 - 2.0 * k / n
+            phi = np.pi * (1.0 + np.sqrt(5.0)) * k
+            rxy = np.sqrt(1.0 - z * z)
+            base = np.stack([rxy * np.cos(phi), rxy * np.sin(phi), z], axis=1)
+            dmin = min(np.linalg.norm(base[a] - base[b]) for a in range(n) for b in range(a + 1, n))
+            base = base / dmin
         base = base - base.mean(axis=0)
         q = rng.standard_normal((walkers, 4))
         q /= np.linalg.norm(q, axis=1, keepdims=True)

@@ -98,6 +98,11 @@ typedef struct fs_config {
      * parallel-path mode, DOF <= 8 and whole warps of walkers; the model is set with
      * fs_set_learned_proposal (until then the network is zero, i.e. the free proposal) */
     int32_t learned;
+    /* 1 = the walkers' paths stay in device memory and the sweep works on them in place
+     * (enableGlobalPath: kernel.py:238-239, kernel.c:62-70, :582-588) instead of staging
+     * each walker in shared memory; for paths larger than shared memory (e.g. 27 DOF x
+     * 1024 slices in FP64).  Same arithmetic and results as the shared-memory sweep. */
+    int32_t global_path;
 } fs_config;
 
 /* fs_query output */
@@ -167,9 +172,10 @@ int fs_sync_timeout(fs_handle *h, double seconds);
 
 /* Raw device results.  Operators: [n_threads][n_ops] per-thread means (FP32 values for
  * FS_ACCUM_REF_FP32 / FS_ACCUM_KAHAN in FP32 builds, else FP64; [..][3] FP64 for
- * FS_ACCUM_STUDY), returned as double.  Correlator: [walkers][n_corr][N/2] running sums
- * since creation / the last fs_zero_accumulators, as double.  Bins: [res^DOF] counts.
- * Histogram: [hist_bins] counts. */
+ * FS_ACCUM_STUDY: plain FP32, Kahan FP32, FP64 sums of the same values), returned as
+ * double.  Correlator: [walkers][n_corr][N/2] running sums since creation / the last
+ * fs_zero_accumulators, as double; FS_ACCUM_STUDY: [..][4] = plain FP32 sum, Kahan sum,
+ * Kahan compensation, FP64 sum.  Bins: [res^DOF] counts.  Histogram: [hist_bins] counts. */
 int fs_get_operators(fs_handle *h, double *out, size_t n);
 int fs_get_correlator(fs_handle *h, double *out, size_t n);
 int fs_get_accepts(fs_handle *h, uint32_t *out, size_t n);
@@ -180,6 +186,17 @@ int fs_zero_accumulators(fs_handle *h);
 int fs_set_correlator(fs_handle *h, const double *in, size_t n);
 int fs_set_bins(fs_handle *h, const uint32_t *in, size_t n);
 int fs_set_histogram(fs_handle *h, const uint64_t *in, size_t n);
+/* Ensemble moments of the correlator over walkers [walker_begin, walker_end), reduced on
+ * the device in FP64 (the host reduction of kernel.py:608-617 for walker counts whose
+ * per-walker array is too large to copy): sum[l][col] and sumsq[l][col] for each lag
+ * l = c * N/2 + tau, col = 0 (one column), or plain FP32, Kahan, FP64 (three columns,
+ * FS_ACCUM_STUDY).  n = n_corr * N/2 * columns. */
+int fs_reduce_correlator(fs_handle *h, int64_t walker_begin, int64_t walker_end, double *sum, double *sumsq,
+                         size_t n);
+/* Fill all walkers' paths from n_template walkers of host data ([n_template][DOF][N] in
+ * the path precision): walker w gets template w % n_template, replicated on the device.
+ * For walker counts whose full path array is impractical to stage in host memory. */
+int fs_set_paths_tiled(fs_handle *h, const void *host, size_t n_template);
 /* device time of the last fs_run call (all its launches), seconds */
 int fs_get_run_time(fs_handle *h, double *seconds);
 

@@ -33,6 +33,11 @@ def nskip_for(lux_in_kernel: int) -> int:
     return _NSKIP.get(lux_in_kernel, lux_in_kernel - 24)
 
 
+# precision-study correlator accumulator: FP64, plain FP32, Kahan sum and compensation
+COR_STUDY_DTYPE = np.dtype([("d", np.float64), ("f", np.float32), ("ks", np.float32), ("kc", np.float32),
+                            ("pad", np.float32)])
+
+
 @dataclass
 class OracleConfig:
     """The reference's KernelArgs fields that the sweep uses (kernel_args.py:23-51)."""
@@ -195,7 +200,7 @@ class OracleSampler:
         op_ft = {0: ft, 1: np.float64, 2: np.float32, 3: np.float64}[c.accum]
         nops = len(c.operators)
         self.op_means = np.zeros((nT, nops, 3) if c.accum == 3 else (nT * max(nops, 1),), op_ft)
-        cor_ft = ft if c.accum == 0 else np.float64
+        cor_ft = ft if c.accum == 0 else (COR_STUDY_DTYPE if c.accum == 3 else np.float64)
         self.cor_means = np.zeros((W, max(len(c.correlators), 1), c.N // 2), cor_ft)
         self.bins = np.zeros(c.binResolutionPerDOF ** c.DOF if c.enableBins else 1, np.uint32)
         self.hist = np.zeros(max(c.histBins, 1), np.uint64)

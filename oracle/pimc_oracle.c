@@ -185,6 +185,13 @@ static inline void fso_kahan_add(fso_kahan_t *k, float x)
     k->s = t;
 }
 
+/* precision-study correlator accumulator (FS_ACCUM 3): the same products summed in
+ * plain FP32, Kahan-compensated FP32 and FP64; 24 bytes, the device's layout */
+typedef struct {
+    double d;
+    float f, ks, kc, pad;
+} fso_cor_study_t;
+
 #if FS_NCOR > 0
 static inline FT fso_cor_prod(const FT *path, uint32_t s1, uint32_t s2, int c)
 {
@@ -269,6 +276,8 @@ int fso_run(fso_args_t *A)
          * on the device, kernel.c:784-788) */
         double cord[FS_NCOR][FS_HALF_N];
         FT corf[FS_NCOR][FS_HALF_N];
+        float cor32[FS_NCOR][FS_HALF_N];
+        fso_kahan_t cork[FS_NCOR][FS_HALF_N];
         {
             size_t crow = (size_t)w;
             for (int c = 0; c < FS_NCOR; c++)
@@ -276,11 +285,19 @@ int fso_run(fso_args_t *A)
                     size_t idx = (crow * FS_NCOR + c) * FS_HALF_N + tau;
 #if FS_ACCUM == 0
                     corf[c][tau] = ((FT *)A->cor_means)[idx];
+#elif FS_ACCUM == 3
+                    const fso_cor_study_t *cs = (const fso_cor_study_t *)A->cor_means + idx;
+                    cord[c][tau] = cs->d;
+                    cor32[c][tau] = cs->f;
+                    cork[c][tau].s = cs->ks;
+                    cork[c][tau].c = cs->kc;
 #else
                     cord[c][tau] = ((double *)A->cor_means)[idx];
 #endif
                 }
         }
+        (void)cor32;
+        (void)cork;
 #endif
         for (int run = 0; run < FS_OPRUNS; run++) {
             for (int step = 0; step < FS_MSTEPS; step++) {
@@ -359,6 +376,13 @@ int fso_run(fso_args_t *A)
                             uint32_t s2 = (s1 + (uint32_t)tau) % FS_N;
                             corf[c][tau] = corf[c][tau] + fso_cor_prod(path, s1, s2, c);
                         }
+#elif FS_ACCUM == 3
+                    for (uint32_t s1 = 0; s1 < FS_N; s1++) {
+                        const FT pr = fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
+                        cor32[c][tau] = cor32[c][tau] + (float)pr;
+                        fso_kahan_add(&cork[c][tau], (float)pr);
+                        cord[c][tau] += (double)pr;
+                    }
 #else
                     for (uint32_t s1 = 0; s1 < FS_N; s1++)
                         cord[c][tau] += (double)fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
@@ -370,6 +394,13 @@ int fso_run(fso_args_t *A)
                     for (int c = 0; c < FS_NCOR; c++) {
 #if FS_ACCUM == 0
                         corf[c][tau] = corf[c][tau] + fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
+#elif FS_ACCUM == 3
+                    {
+                        const FT pr = fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
+                        cor32[c][tau] = cor32[c][tau] + (float)pr;
+                        fso_kahan_add(&cork[c][tau], (float)pr);
+                        cord[c][tau] += (double)pr;
+                    }
 #else
                         cord[c][tau] += (double)fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
 #endif
@@ -418,6 +449,13 @@ int fso_run(fso_args_t *A)
                 size_t idx = ((size_t)w * FS_NCOR + c) * FS_HALF_N + tau;
 #if FS_ACCUM == 0
                 ((FT *)A->cor_means)[idx] = corf[c][tau];
+#elif FS_ACCUM == 3
+                fso_cor_study_t *cs = (fso_cor_study_t *)A->cor_means + idx;
+                cs->d = cord[c][tau];
+                cs->f = cor32[c][tau];
+                cs->ks = cork[c][tau].s;
+                cs->kc = cork[c][tau].c;
+                cs->pad = 0.f;
 #else
                 ((double *)A->cor_means)[idx] = cord[c][tau];
 #endif

@@ -58,9 +58,11 @@ def test_xorshift_stream_bit_exact():
 
 
 # ---------------------------------------------------------------- sweeps vs reference
+@pytest.mark.parametrize("global_path", [True, False], ids=["global_path", "shared_path"])
 @pytest.mark.parametrize("case", sweep_cases())
-def test_sweep_matches_reference_kernel(case):
+def test_sweep_matches_reference_kernel(case, global_path):
     ka, rec = load_sweep(case)
+    ka = dict(ka, enableGlobalPath=global_path)
     k = kernel_for_case(ka, compat=True, accumulation="fp32", fast=False)
     k.setPaths(rec["paths0"])
     if ka["enableRanlux"]:
@@ -83,10 +85,7 @@ def test_sweep_matches_reference_kernel(case):
             np.testing.assert_allclose(k.getPaths(), rec[f"paths{it}"], rtol=1e-4, atol=1e-5)
             raw = k._raw_operators()
             np.testing.assert_allclose(raw, rec[f"ops{it}"], rtol=1e-4, atol=1e-5)
-            n = rec[f"cor{it}"].size
-            cor = np.empty(n, np.float64)
-            from feynsimul_gb300 import _lib
-            _lib.check(_lib.lib().fs_get_correlator(k._handle, cor.ctypes.data, n), k._handle)
+            cor = k._raw_correlator()
             np.testing.assert_allclose(cor.reshape(rec[f"cor{it}"].shape), rec[f"cor{it}"], rtol=1e-4, atol=1e-4)
             assert np.abs(k.getBinCountsRaw().astype(np.int64) - rec[f"bins{it}"].astype(np.int64)).sum() <= 2
     k.close()
@@ -102,12 +101,21 @@ FIXED_CASES = {
 }
 
 
+def _oracle_correlator(o, accum):
+    """The oracle's correlator sums in the layout fs_get_correlator returns."""
+    if accum == 3:
+        c = o.cor_means
+        return np.stack([c["f"], c["ks"], c["kc"], c["d"]], axis=-1).astype(np.float64).reshape(-1)
+    return o.cor_means.astype(np.float64).reshape(-1)
+
+
+@pytest.mark.parametrize("global_path", [False, True], ids=["shared_path", "global_path"])
 @pytest.mark.parametrize("case", sorted(FIXED_CASES))
 @pytest.mark.parametrize("accum", [1, 0, 2, 3])
-def test_fixed_mode_matches_oracle(case, accum):
+def test_fixed_mode_matches_oracle(case, accum, global_path):
     from oracle import oracle as orc
     ka, rec = load_sweep(case)
-    ka = dict(ka, **FIXED_CASES[case])
+    ka = dict(ka, enableGlobalPath=global_path, **FIXED_CASES[case])
     accname = {0: "fp32", 1: "fp64", 2: "kahan", 3: "study"}[accum]
     k = kernel_for_case(ka, compat=False, accumulation=accname, fast=False)
     o = orc.OracleSampler(oracle_config(ka, compat=False, accum=accum))
@@ -146,6 +154,11 @@ def test_fixed_mode_matches_oracle(case, accum):
             np.testing.assert_allclose(k.getPaths(), o.paths, rtol=1e-4, atol=1e-5)
             raw = k._raw_operators()
             np.testing.assert_allclose(raw, o.op_means.reshape(-1)[:raw.size], rtol=1e-4, atol=1e-5)
+            if ka["enableCorrelator"]:
+                cor = k._raw_correlator()
+                want = _oracle_correlator(o, accum)
+                assert cor.size == want.size
+                np.testing.assert_allclose(cor, want, rtol=1e-4, atol=1e-4)
             assert np.array_equal(k.getBinCountsRaw(), o.bins) or \
                 np.abs(k.getBinCountsRaw().astype(np.int64) - o.bins.astype(np.int64)).sum() <= 2
     k.close()

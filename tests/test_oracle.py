@@ -89,3 +89,36 @@ def test_oracle_against_live_reference():
     assert np.array_equal(o.seeds, r.k._seeds.arr)
     assert np.array_equal(o.accepts, r.k._accepts.arr)
     assert np.array_equal(o.paths, r.k._paths.arr)
+
+
+@pytest.mark.parametrize("case", ["xorshift_walker", "xorshift_parallel"])
+def test_oracle_study_correlator_columns(case):
+    """Precision-study accumulation sums the same products three ways on one trajectory:
+    its FP64 column equals the FP64 mode's sums bit for bit, and in walker mode (where the
+    FP32 mode also adds slices in ascending order) its plain-FP32 column equals the FP32
+    mode's sums bit for bit; the Kahan column lies between in error."""
+    ka, _ = load_sweep(case)
+    rng = np.random.RandomState(5)
+    outs = {}
+    for accum in (0, 1, 3):
+        o = orc.OracleSampler(oracle_config(ka, compat=False, accum=accum))
+        if accum == 0:
+            p0 = (rng.randn(*o.paths.shape) * 0.4).astype(o.paths.dtype)
+            s0 = rng.randint(0, 2 ** 31 - 1, size=o.seeds.shape).astype(np.uint32)
+            w0 = rng.randint(0, 2 ** 31 - 1, size=o.walker_seeds.shape).astype(np.uint32)
+        o.paths[...] = p0
+        o.seeds[...] = s0
+        o.walker_seeds[...] = w0
+        for _ in range(3):
+            o.run()
+        outs[accum] = o
+    st = outs[3].cor_means
+    assert np.array_equal(outs[3].paths, outs[1].paths)
+    assert np.array_equal(st["d"], outs[1].cor_means)
+    if not ka["enableParallelizePath"]:
+        assert np.array_equal(st["f"], outs[0].cor_means)
+    ref = st["d"]
+    err_f = np.abs(st["f"].astype(np.float64) - ref).max()
+    err_k = np.abs(st["ks"].astype(np.float64) - ref).max()
+    assert err_k <= err_f + 1e-12
+    assert err_f <= 1e-5 * np.abs(ref).max()
