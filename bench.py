@@ -221,8 +221,8 @@ def integrated_autocorr(series):
 
 
 # register budget the sweep kernel is compiled for, per workload (launch-shape sweep on GB300)
-TUNED_MIN_BLOCKS = {"he3": 4, "ho": 0}
-TUNED_WPB = {"he3": 8, "ho": 0}
+TUNED_MIN_BLOCKS = {"he3": 7, "ho": 0}
+TUNED_WPB = {"he3": 4, "ho": 0}
 
 
 # ------------------------------------------------------------------ roofline

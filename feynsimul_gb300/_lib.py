@@ -53,7 +53,7 @@ class FsConfig(ctypes.Structure):
         ("hist_lo", ctypes.c_double), ("hist_hi", ctypes.c_double), ("hist_bins", ctypes.c_int32),
         ("compat", ctypes.c_int32), ("accum", ctypes.c_int32), ("fast_math", ctypes.c_int32),
         ("walkers_per_block", ctypes.c_int32), ("min_blocks_per_sm", ctypes.c_int32),
-        ("learned", ctypes.c_int32), ("global_path", ctypes.c_int32),
+        ("learned", ctypes.c_int32), ("global_path", ctypes.c_int32), ("potential_cache", ctypes.c_int32),
     ]
 
 

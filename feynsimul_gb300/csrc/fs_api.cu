@@ -66,7 +66,7 @@ struct fs_handle {
     std::vector<std::string> ops, cors, hists;
     // launch geometry
     int tpw = 1, seg = 1, wpb = 1, block = 1, grid = 1;
-    long long wstride = 0;
+    long long wstride = 0, vstride = 0;
     long long n_threads = 0;
     size_t smem = 0;
     int regs = 0;
@@ -309,7 +309,7 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << lit(c.beta / (double)c.n_slices) << "\n#define FS_OPNORM " << lit(opnorm)
       << "\n#define FS_BINS " << (c.enable_bins ? 1 : 0) << "\n#define FS_NHIST " << nhist
       << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n#define FS_GLOBAL " << (c.global_path ? 1 : 0)
-      << "\n";
+      << "\n#define FS_VCACHE " << (h.vstride ? 1 : 0) << "\n#define FS_VSTRIDE " << h.vstride << "\n";
     {
         char b[64];
         snprintf(b, sizeof b, "%.9E", (double)(c.ranlux_int_max + 1ull));
@@ -586,8 +586,14 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     if ((wstride / 16) % 2 == 0) wstride += 16;
     if (c.global_path) wstride = (long long)c.dof * c.n_slices;  // no shared-memory path
     h->wstride = wstride;
-    const size_t per_walker =
+    // potential cache: one value per slice in the path's padded slice layout, walker stride
+    // an odd multiple of 16 words
+    long long vstride = ((dstride + 15) / 16) * 16;
+    if ((vstride / 16) % 2 == 0) vstride += 16;
+    const size_t per_walker_base =
         (size_t)((c.global_path ? 0 : wstride) + (long long)h->cors.size() * c.n_slices) * h->ft;
+    h->vstride = c.potential_cache == 2 ? 0 : vstride;
+    size_t per_walker = per_walker_base + (size_t)h->vstride * h->ft;
     const size_t hist_bytes = (size_t)(c.hist_bins > 0 && !h->hists.empty() ? c.hist_bins : 0) * 4;
     if (c.walkers_per_block > 0) {
         h->wpb = c.walkers_per_block;
@@ -624,6 +630,19 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     }
     h->grid = (c.n_walkers + h->wpb - 1) / h->wpb;
     h->smem = per_walker * h->wpb + hist_bytes;
+    if (h->vstride && c.potential_cache == 0) {
+        // automatic: the cache halves the potential evaluations but takes shared memory;
+        // keep it where it costs no resident CTA per SM, or where the potential is large
+        // (more than 8 DOF: a cluster of 4+ atoms)
+        auto ctas = [](size_t smem) { return (227ll * 1024) / (long long)(smem + 1024); };
+        const size_t without = per_walker_base * h->wpb + hist_bytes;
+        if (ctas(h->smem) < std::min(ctas(without), 2048ll / h->block) && c.dof <= 8) h->vstride = 0;
+    }
+    if (h->smem > 227 * 1024 && h->vstride && c.potential_cache != 1) h->vstride = 0;  // no room
+    if (!h->vstride) {
+        per_walker = per_walker_base;
+        h->smem = per_walker * h->wpb + hist_bytes;
+    }
     // Register budget: unless the caller fixes it, compile for as many CTAs per SM as shared
     // memory admits (<= 2048 threads per SM, >= 64 registers per thread).  Without the bound
     // the compiler spends registers freely and the large kernels drop to one CTA per SM.

@@ -44,6 +44,10 @@
 #define FS_DSTRIDE (FS_N + (FS_N >> FS_S))
 #endif
 #define FS_AT(P, d, s) (P)[(d) * FS_DSTRIDE + FS_PHYS(s)]
+#ifndef FS_VCACHE
+#define FS_VCACHE 0
+#define FS_VSTRIDE 0
+#endif
 
 #if FS_DOUBLE
 #define FS_ADD __dadd_rn
@@ -136,8 +140,14 @@ __device__ __forceinline__ fs_u32 fs_offset(FsIStream &g, fs_u32 range)
 // action exactly; the Metropolis-Hastings log-ratio therefore gains only, per degree of
 // freedom of that node, [(x_old - mid)^2 - (x_new - mid)^2] / (2 sigma_1^2)
 // + [z_new^2 - ((x_old - lmu) / lsd)^2] / 2, with z_new the standard normal drawn.
-__device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, const FT *sigma, const FT *lmu,
-                                         const FT *lsd)
+//
+// Potential cache (FS_VCACHE): Vc holds V(x_s) of every slice of the walker's current path
+// (same padded slice layout as the path).  The old action is then a sum of cached values
+// -- the same products and sums as evaluating V again, so bit for bit the same aOld --
+// and only the proposed nodes are evaluated; an accepted move leaves their new values in
+// the cache, a rejected one restores the path and re-evaluates its nodes.
+__device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream &g, const FT *sigma,
+                                         const FT *lmu, const FT *lsd)
 {
     FT corr = (FT)0;
     FT old[FS_OLD_N];
@@ -151,7 +161,11 @@ __device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, cons
     FS_MOVE_UNROLL
     for (int i = 1; i < FS_SEG; i++) {
         const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
+#if FS_VCACHE
+        aOld = FS_ADD(aOld, FS_MUL((FT)FS_EPS, Vc[FS_PHYS(p)]));
+#else
         aOld = FS_ADD(aOld, FS_MUL((FT)FS_EPS, fs_pot(FS_ARGS_AT(P, p))));
+#endif
     }
     FS_MOVE_UNROLL
     for (int n = 1; n <= FS_S; n++) {
@@ -203,7 +217,11 @@ __device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, cons
     FS_MOVE_UNROLL
     for (int i = 1; i < FS_SEG; i++) {
         const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
-        aNew = FS_ADD(aNew, FS_MUL((FT)FS_EPS, fs_pot(FS_ARGS_AT(P, p))));
+        const FT v = fs_pot(FS_ARGS_AT(P, p));
+#if FS_VCACHE
+        Vc[FS_PHYS(p)] = v;
+#endif
+        aNew = FS_ADD(aNew, FS_MUL((FT)FS_EPS, v));
     }
     const FT acc = fs_uniform(g);
 #if FS_LEARNED
@@ -220,6 +238,15 @@ __device__ __forceinline__ int fs_bisect(FT *P, fs_u32 start, FsUStream &g, cons
 #pragma unroll
             for (int d = 0; d < FS_DOF; d++) FS_AT(P, d, p) = old[(i - 1) * FS_DOF + d];
         }
+#if FS_VCACHE
+        FS_MOVE_UNROLL
+        for (int i = 1; i < FS_SEG; i++) {
+            const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
+            Vc[FS_PHYS(p)] = fs_pot(FS_ARGS_AT(P, p));
+        }
+#else
+        (void)Vc;
+#endif
         return 0;
     }
     return 1;
@@ -288,11 +315,12 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     __shared__ fs_u32 s_off[FS_WPB];
 #endif
 #if FS_GLOBAL
-    FT *s_cor = (FT *)fs_smem;                                   // [WPB][NCOR][N]
+    FT *s_v = (FT *)fs_smem;                                     // [WPB][VSTRIDE] (FS_VCACHE)
 #else
     FT *s_path = (FT *)fs_smem;                                  // [WPB][DOF*N]
-    FT *s_cor = s_path + FS_WPB * FS_WSTRIDE;                    // [WPB][NCOR][N]
+    FT *s_v = s_path + FS_WPB * FS_WSTRIDE;                      // [WPB][VSTRIDE] (FS_VCACHE)
 #endif
+    FT *s_cor = s_v + FS_WPB * FS_VSTRIDE;                       // [WPB][NCOR][N]
     fs_u32 *s_hist = (fs_u32 *)(s_cor + FS_WPB * FS_NCOR * FS_N);  // [HBINS]
 
     const int tid_b = threadIdx.x;
@@ -334,6 +362,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #else
         FT *P = s_path + wl * FS_WSTRIDE;
 #endif
+        FT *Vc = s_v + wl * FS_VSTRIDE;
         const int tid = fs_thread_id(w, t);
         // sigma table (kernel.c:608-618), computed on the host with the same FP operations
         const FT *sigma = fs_sigma;
@@ -399,6 +428,20 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #endif
 #endif
 
+#if FS_VCACHE
+        // potential cache: V of each of the walker's slices at launch start
+        {
+#if FS_PARALLEL
+            const int v_lo = t * FS_SEG, v_hi = (t + 1) * FS_SEG;
+#else
+            const int v_lo = 0, v_hi = FS_N;
+#endif
+#pragma unroll 1
+            for (int s = v_lo; s < v_hi; s++) Vc[FS_PHYS(s)] = fs_pot(FS_ARGS_AT(P, s));
+        }
+        FS_WSYNC();
+#endif
+
         // ---- sweeps (kernel.c:628-799) ----
 #pragma unroll 1
         for (int run = 0; run < FS_OPRUNS; run++) {
@@ -444,9 +487,9 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                         lsd[d] = s1 * __expf(0.5f * sv);
                     }
                 }
-                n_acc += (fs_u32)fs_bisect(P, start, fs, sigma, lmu, lsd);
+                n_acc += (fs_u32)fs_bisect(P, Vc, start, fs, sigma, lmu, lsd);
 #else
-                n_acc += (fs_u32)fs_bisect(P, start, fs, sigma, nullptr, nullptr);
+                n_acc += (fs_u32)fs_bisect(P, Vc, start, fs, sigma, nullptr, nullptr);
 #endif
                 FS_WSYNC();
             }

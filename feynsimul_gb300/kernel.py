@@ -197,6 +197,8 @@ class PIMCKernel:
         # enableGlobalOldPath (kernel.c:259-276) has no counterpart: the saved old segment
         # is per-thread private data either way (registers, spilling to local memory)
         c.global_path = int(bool(self._enableGlobalPath)) if self._enableBisection else 0
+        pc = getattr(ka, "potentialCache", None)
+        c.potential_cache = 0 if pc is None else (1 if pc else 2)
         self._learned = bool(c.learned)
         self._cfg = c
 

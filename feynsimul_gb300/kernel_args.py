@@ -20,6 +20,9 @@ Keyword-only additions of this engine:
 * ``learnedProposal`` (False): draw each segment's level-1 midpoint from a learned Gaussian
   (feynsimul_gb300.learned), Metropolis-Hastings corrected; load the model with
   PIMCKernel.setLearnedProposal.
+* ``potentialCache`` (None = automatic): keep V of every slice in shared memory so a move
+  evaluates the potential only at its proposed nodes (bit-identical results; costs
+  shared memory, i.e. occupancy).
 * ``seed`` (None): master seed for the seed tables; None draws from ``np.random`` exactly
   as kernel.py:412-426 does.
 """
@@ -66,6 +69,7 @@ class KernelArgs:
                  walkersPerBlock=0,
                  minBlocksPerSM=0,
                  learnedProposal=False,
+                 potentialCache=None,
                  seed=None):
         self.system = system
         self.nbrOfWalkers = nbrOfWalkers
@@ -105,4 +109,5 @@ class KernelArgs:
         self.walkersPerBlock = walkersPerBlock
         self.minBlocksPerSM = minBlocksPerSM
         self.learnedProposal = learnedProposal
+        self.potentialCache = potentialCache
         self.seed = seed

@@ -47,8 +47,16 @@ X1_ADD, X2_ADD = 1.003535949, 1.454790369
 GROUND_STATES = [0.0872, 0.387, 0.901, 1.605, 2.478, 3.489, 4.641, 5.904]
 
 
-def lm2m2_c_code(reference_derivative: bool = False) -> str:
-    """C source of lm2m2_r2(r^2) [K] and dlm2m2_dr2(r^2) = dV/d(r^2) [K / Angstrom^2]."""
+def lm2m2_c_code(reference_derivative: bool = False, branchless: bool = True) -> str:
+    """C source of lm2m2_r2(r^2) [K] and dlm2m2_dr2(r^2) = dV/d(r^2) [K / Angstrom^2].
+
+    ``branchless`` (default) evaluates every term and selects, so the lanes of a warp
+    never diverge on a pair's distance regime: one rsqrt gives r and 1/x^2, the damping
+    exp(-(D/x - 1)^2) is taken with D/x - 1 clamped at 0 (F = 1 beyond D), and the add-on
+    Aa (sin(B(x - x1) - pi/2) + 1) = Aa (1 - cos(B(x - x1))) is masked outside [x1, x2].
+    ``branchless=False`` gives the reference-shaped form with branches (lm2m2.h:22-147)."""
+    if branchless:
+        return _lm2m2_c_code_branchless(reference_derivative)
     add_term = "(cs * B + 1.0)" if reference_derivative else "(cs * B)"
     return f"""
 inline FLOAT_TYPE fs_sq(FLOAT_TYPE v) {{ return v * v; }}
@@ -100,6 +108,48 @@ inline FLOAT_TYPE dlm2m2_dr2(FLOAT_TYPE r2)
         dv = dv + {A_ADD!r} * {add_term};
     }}
     return {EPS_K!r} * dv / ({2.0 * RM!r} * r);
+}}
+"""
+
+
+def _lm2m2_c_code_branchless(reference_derivative: bool) -> str:
+    rm2 = RM * RM
+    dr = D_CUT * RM
+    tiny = 0.0005
+    B = 2.0 * np.pi / (X2_ADD - X1_ADD)
+    # reference form of the add-on derivative term: Aa (cos(...) B + 1) = Aa (B sin(w) + 1)
+    add_d = f"({A_ADD!r} * ({B!r} * sw + 1.0))" if reference_derivative else f"({A_ADD * B!r} * sw)"
+    return f"""
+inline FLOAT_TYPE fs_sq(FLOAT_TYPE v) {{ return v * v; }}
+inline FLOAT_TYPE lm2m2_r2(FLOAT_TYPE r2)
+{{
+    FLOAT_TYPE ir = rsqrt(r2);
+    FLOAT_TYPE x = r2 * ir * {1.0 / RM!r};
+    FLOAT_TYPE ix2 = {rm2!r} * (ir * ir);
+    FLOAT_TYPE rat = ((({C10!r} * ix2 + {C8!r}) * ix2) + {C6!r}) * ix2 * ix2 * ix2;
+    FLOAT_TYPE q = fmax({dr!r} * ir - 1.0, 0.0);
+    rat = (r2 > {tiny * tiny!r}) ? rat * exp(-q * q) : 0.0;
+    FLOAT_TYPE w = {B!r} * (x - {X1_ADD!r});
+    FLOAT_TYPE add = (x >= {X1_ADD!r} && x <= {X2_ADD!r}) ? {A_ADD!r} : 0.0;
+    return {EPS_K!r} * ({A_STAR!r} * exp(x * ({BETA_STAR!r} * x - {ALPHA!r})) - rat + add * (1.0 - cos(w)));
+}}
+inline FLOAT_TYPE dlm2m2_dr2(FLOAT_TYPE r2)
+{{
+    FLOAT_TYPE ir = rsqrt(r2);
+    FLOAT_TYPE x = r2 * ir * {1.0 / RM!r};
+    FLOAT_TYPE ix = {RM!r} * ir;
+    FLOAT_TYPE ix2 = ix * ix;
+    FLOAT_TYPE ix6 = ix2 * ix2 * ix2;
+    FLOAT_TYPE rat = (({C10!r} * ix2 + {C8!r}) * ix2 + {C6!r}) * ix6;
+    FLOAT_TYPE drat = -((({10.0 * C10!r} * ix2 + {8.0 * C8!r}) * ix2 + {6.0 * C6!r}) * ix6 * ix);
+    FLOAT_TYPE q = fmax({D_CUT!r} * ix - 1.0, 0.0);
+    FLOAT_TYPE F = exp(-q * q);
+    FLOAT_TYPE dfr = (r2 > {tiny * tiny!r}) ? F * drat + F * (2.0 * q * {D_CUT!r} * ix2) * rat : 0.0;
+    FLOAT_TYPE sw = sin({B!r} * (x - {X1_ADD!r}));
+    FLOAT_TYPE inwin = (x >= {X1_ADD!r} && x <= {X2_ADD!r}) ? 1.0 : 0.0;
+    FLOAT_TYPE dv = {A_STAR!r} * exp(x * ({BETA_STAR!r} * x - {ALPHA!r})) * ({2.0 * BETA_STAR!r} * x - {ALPHA!r})
+                    - dfr + inwin * {add_d};
+    return {EPS_K!r} * dv * ir * {0.5 / RM!r};
 }}
 """
 

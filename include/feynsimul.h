@@ -103,6 +103,10 @@ typedef struct fs_config {
      * each walker in shared memory; for paths larger than shared memory (e.g. 27 DOF x
      * 1024 slices in FP64).  Same arithmetic and results as the shared-memory sweep. */
     int32_t global_path;
+    /* new: potential cache (V of every slice kept in shared memory, so a move evaluates the
+     * potential only at its proposed nodes): 0 = automatic, 1 = on, 2 = off.  Results are
+     * bit-identical either way; it trades shared memory (occupancy) for potential work. */
+    int32_t potential_cache;
 } fs_config;
 
 /* fs_query output */

@@ -39,6 +39,10 @@
 #include <stdlib.h>
 #include <string.h>
 #include <tgmath.h>
+/* OpenCL's rsqrt for plugin code (type-generic through tgmath's sqrt) */
+#ifndef rsqrt
+#define rsqrt(x) (1 / sqrt(x))
+#endif
 
 #include "rng_oracle.h"
 

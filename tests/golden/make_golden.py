@@ -9,6 +9,8 @@ RANLUXCL header on the CPU (oracle/build_ref.py) and records inputs and outputs:
 
 * ``ranlux_streams.npz``: RANLUXCL uniforms and final 28-word states for luxury levels
   0-4 and p=124, FP32 and FP64 variants (pyopencl-ranluxcl.cl:384-557, :597-725, :893-920);
+* ``lm2m2_ref.npz``: the reference's LM2M2 pair potential and derivative routine
+  (physical_systems/lm2m2.h) on a grid of pair distances;
 * ``sweep_<case>.npz``: initial paths and seed tables, and after each of two
   ``metropolis`` launches: paths, accept counts, seed / RANLUX tables, operator means,
   correlator sums and histogram bins (kernel.c:514-837).
@@ -106,10 +108,26 @@ def make_sweep(name, ka):
     np.savez_compressed(os.path.join(HERE, f"sweep_{name}.npz"), **rec)
 
 
+def make_lm2m2():
+    """``lm2m2_ref.npz``: the reference's pair potential lm2m2sqrt(r^2) and its derivative
+    routine dlm2m2sqrtdr(r^2) (physical_systems/lm2m2.h), built as-is in FP64 and FP32, on a
+    grid of r from 0.3 to 20 Angstrom."""
+    libs = br.lm2m2_header_lib()
+    r = np.concatenate([np.linspace(0.3, 2.5, 221), np.linspace(2.5, 6.0, 3501)[1:], np.linspace(6.0, 20.0, 141)[1:]])
+    out = {"r": r}
+    for ft, dt in (("double", np.float64), ("float", np.float32)):
+        sr = np.ascontiguousarray((r * r).astype(dt))
+        v, dv = np.zeros_like(sr), np.zeros_like(sr)
+        libs[ft].ref_lm2m2(sr.ctypes.data, v.ctypes.data, dv.ctypes.data, len(sr))
+        out[f"r2_{ft}"], out[f"v_{ft}"], out[f"dv_{ft}"] = sr, v, dv
+    np.savez_compressed(os.path.join(HERE, "lm2m2_ref.npz"), **out)
+
+
 def main():
     if not br.reference_available():
         raise SystemExit("reference tree not present; fixtures are generated where it is")
     make_ranlux()
+    make_lm2m2()
     for name, ka in CASES.items():
         make_sweep(name, ka)
         print("wrote", name)

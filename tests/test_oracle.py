@@ -122,3 +122,73 @@ def test_oracle_study_correlator_columns(case):
     err_k = np.abs(st["ks"].astype(np.float64) - ref).max()
     assert err_k <= err_f + 1e-12
     assert err_f <= 1e-5 * np.abs(ref).max()
+
+
+def _golden_lm2m2():
+    import os
+    from golden_cases import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "lm2m2_ref.npz"))
+    return {k: z[k] for k in z.files}
+
+
+def test_lm2m2_numpy_matches_reference_header():
+    """The LM2M2 restatement against the reference's lm2m2.h built as-is (golden)."""
+    from feynsimul_gb300.physical_systems.lm2m2 import lm2m2_numpy
+    g = _golden_lm2m2()
+    r = np.sqrt(g["r2_double"])
+    v, dv_ref_form = lm2m2_numpy(r, reference_derivative=True)
+    np.testing.assert_allclose(v, g["v_double"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(dv_ref_form, g["dv_double"], rtol=1e-12, atol=1e-12)
+    # the correct derivative equals d/d(r^2) of the potential (numerically)
+    _, dv = lm2m2_numpy(r)
+    r2, h = g["r2_double"], 1e-6 * g["r2_double"]
+    num = (lm2m2_numpy(np.sqrt(r2 + h))[0] - lm2m2_numpy(np.sqrt(r2 - h))[0]) / (2 * h)
+    np.testing.assert_allclose(dv, num, rtol=1e-5, atol=1e-8)
+
+
+def _plugin_c_lib(code, ft):
+    import ctypes
+    import hashlib
+    import os
+    import subprocess
+    import tempfile
+    src = ("#include <tgmath.h>\n#define FLOAT_TYPE %s\n#define rsqrt(x) (1 / sqrt(x))\n%s\n"
+           "void eval(const FLOAT_TYPE *r2, FLOAT_TYPE *v, FLOAT_TYPE *dv, int n)\n"
+           "{ for (int i = 0; i < n; i++) { v[i] = lm2m2_r2(r2[i]); dv[i] = dlm2m2_dr2(r2[i]); } }\n") % (ft, code)
+    d = tempfile.mkdtemp(prefix="fs_lm2m2_")
+    h = hashlib.sha1(src.encode()).hexdigest()[:12]
+    c, so = os.path.join(d, f"p{h}.c"), os.path.join(d, f"p{h}.so")
+    open(c, "w").write(src)
+    flags = ["-std=gnu11", "-O2", "-ffp-contract=off", "-fgnu89-inline", "-fPIC", "-shared", "-w"]
+    if ft == "float":
+        flags.append("-fsingle-precision-constant")
+    subprocess.run(["gcc", *flags, c, "-o", so, "-lm"], check=True)
+    lib = ctypes.CDLL(so)
+    lib.eval.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int]
+    return lib
+
+
+@pytest.mark.parametrize("branchless", [True, False])
+@pytest.mark.parametrize("reference_derivative", [False, True])
+def test_lm2m2_plugin_code_matches_restatement(branchless, reference_derivative):
+    """The plugin's C code (as pasted into the sweep kernel) against the numpy restatement,
+    in FP64 to 1e-12 and in FP32 to FP32 rounding."""
+    from feynsimul_gb300.physical_systems.lm2m2 import lm2m2_c_code, lm2m2_numpy
+    g = _golden_lm2m2()
+    code = lm2m2_c_code(reference_derivative, branchless=branchless)
+    r2 = np.ascontiguousarray(g["r2_double"])
+    want_v, want_dv = lm2m2_numpy(np.sqrt(r2), reference_derivative=reference_derivative)
+    lib = _plugin_c_lib(code, "double")
+    v, dv = np.zeros_like(r2), np.zeros_like(r2)
+    lib.eval(r2.ctypes.data, v.ctypes.data, dv.ctypes.data, len(r2))
+    np.testing.assert_allclose(v, want_v, rtol=1e-11, atol=1e-11)
+    np.testing.assert_allclose(dv, want_dv, rtol=1e-11, atol=1e-11)
+    r2f = np.ascontiguousarray(r2.astype(np.float32))
+    libf = _plugin_c_lib(code, "float")
+    vf, dvf = np.zeros_like(r2f), np.zeros_like(r2f)
+    libf.eval(r2f.ctypes.data, vf.ctypes.data, dvf.ctypes.data, len(r2f))
+    # FP32: the repulsive and dispersion terms cancel near r_m, so the error is relative
+    # to the terms (a few K there), not to V
+    assert np.all(np.abs(vf - want_v) <= 2e-6 * np.abs(want_v) + 5e-4)
+    sel = np.sqrt(r2) > 2.2
+    np.testing.assert_allclose(dvf[sel], want_dv[sel], rtol=1e-4, atol=5e-3)
