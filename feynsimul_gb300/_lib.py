@@ -36,8 +36,10 @@ EXPORTS = (
     "fs_mlp_pack", "fs_mlp_infer", "fs_set_learned_proposal", "fs_batch_create", "fs_batch_destroy",
     "fs_batch_run", "fs_batch_sync", "fs_batch_get_run_time", "fs_batch_set_paths", "fs_batch_get_paths",
     "fs_batch_set_seeds", "fs_batch_get_op_sums", "fs_batch_get_accepts", "fs_batch_query",
-    "fs_reduce_correlator", "fs_set_paths_tiled",
+    "fs_reduce_correlator", "fs_set_paths_tiled", "fs_get_step_counter", "fs_set_step_counter",
 )
+
+FS_MOVE_BISECTION, FS_MOVE_PATH_SHIFT, FS_MOVE_SINGLE_NODE = 1, 2, 4
 
 
 class FsConfig(ctypes.Structure):
@@ -54,6 +56,7 @@ class FsConfig(ctypes.Structure):
         ("compat", ctypes.c_int32), ("accum", ctypes.c_int32), ("fast_math", ctypes.c_int32),
         ("walkers_per_block", ctypes.c_int32), ("min_blocks_per_sm", ctypes.c_int32),
         ("learned", ctypes.c_int32), ("global_path", ctypes.c_int32), ("potential_cache", ctypes.c_int32),
+        ("moves", ctypes.c_int32), ("alpha", ctypes.c_double), ("ps_alpha", ctypes.c_double),
     ]
 
 
@@ -110,6 +113,8 @@ _PROTOS = {
     "fs_get_correlator": ([_P, _P, _S], ctypes.c_int),
     "fs_reduce_correlator": ([_P, ctypes.c_int64, ctypes.c_int64, _P, _P, _S], ctypes.c_int),
     "fs_set_paths_tiled": ([_P, _P, _S], ctypes.c_int),
+    "fs_get_step_counter": ([_P, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+    "fs_set_step_counter": ([_P, ctypes.c_uint64], ctypes.c_int),
     "fs_get_accepts": ([_P, _P, _S], ctypes.c_int),
     "fs_get_bins": ([_P, _P, _S], ctypes.c_int),
     "fs_get_histogram": ([_P, _P, _S], ctypes.c_int),

@@ -73,6 +73,8 @@ struct fs_handle {
     size_t ft = 4, op_elem = 8, cor_elem = 8;
     size_t n_ops_elems = 0, n_cor_elems = 0, n_cor_lags = 0, n_bins = 0, n_hist = 0;
     double *d_red = nullptr;  // fs_reduce_correlator output (sum, sumsq)
+    void *d_shift_old = nullptr;  // path shift, fixed mode: row saved before the move
+    unsigned long long steps_done = 0;  // Metropolis steps of all launches so far
     // CUDA objects
     cudaLibrary_t lib = nullptr;
     cudaKernel_t k_metro = nullptr, k_rinit = nullptr;
@@ -311,6 +313,14 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n#define FS_GLOBAL " << (c.global_path ? 1 : 0)
       << "\n#define FS_VCACHE " << (h.vstride ? 1 : 0) << "\n#define FS_VSTRIDE " << h.vstride << "\n";
     {
+        const int mv = c.moves ? c.moves : FS_MOVE_BISECTION;
+        const double nb = (double)c.n_slices / c.beta;
+        o << "#define FS_BISECT " << ((mv & FS_MOVE_BISECTION) ? 1 : 0) << "\n#define FS_PATH_SHIFT "
+          << ((mv & FS_MOVE_PATH_SHIFT) ? 1 : 0) << "\n#define FS_SNM " << ((mv & FS_MOVE_SINGLE_NODE) ? 1 : 0)
+          << "\n#define FS_EPS_INV2 " << lit(nb * nb) << "\n#define FS_ALPHA " << lit(c.alpha)
+          << "\n#define FS_PSALPHA " << lit(c.ps_alpha) << "\n";  // kernel.py:298-299, :326, :329
+    }
+    {
         char b[64];
         snprintf(b, sizeof b, "%.9E", (double)(c.ranlux_int_max + 1ull));
         o << "#define FS_RIM " << b << "f\n";  // kernel.py:334: always a float literal
@@ -528,6 +538,15 @@ static int validate(const fs_config &c, int nops, int ncor, int nhist)
     }
     if (c.min_blocks_per_sm < 0 || c.min_blocks_per_sm > 32)
         return fail(nullptr, FS_ERR_CONFIG, "min_blocks_per_sm must be in [0, 32]");
+    if (c.moves < 0 || c.moves > 7) return fail(nullptr, FS_ERR_CONFIG, "moves must be a mask of FS_MOVE_*");
+    if (c.enable_parallelize_path && (c.moves & FS_MOVE_SINGLE_NODE))
+        return fail(nullptr, FS_ERR_CONFIG, "Single node move not possible when enableParallelizePath is True.");
+    if (c.enable_parallelize_path && (c.moves & FS_MOVE_PATH_SHIFT))
+        return fail(nullptr, FS_ERR_CONFIG, "Shift path not possible when enableParallelizePath is True.");
+    if (c.enable_parallelize_path && c.moves && !(c.moves & FS_MOVE_BISECTION))
+        return fail(nullptr, FS_ERR_CONFIG, "parallel-path mode needs the bisection move");
+    if (c.learned && c.moves && c.moves != FS_MOVE_BISECTION)
+        return fail(nullptr, FS_ERR_CONFIG, "the learned proposal goes with the bisection move only");
     return FS_OK;
 }
 
@@ -535,7 +554,7 @@ static void free_buffers(fs_handle *h)
 {
     void *bufs[] = {h->d_paths, h->d_accepts, h->d_seeds, h->d_snap, h->d_wseeds, h->d_rtab,
                     h->d_gtab, h->d_bins, h->d_ops, h->d_cor, h->d_hist, h->d_status,
-                    h->d_mlp_frag, h->d_mlp_bias, h->d_red};
+                    h->d_mlp_frag, h->d_mlp_bias, h->d_red, h->d_shift_old};
     for (void *p : bufs)
         if (p) cudaFree(p);
 }
@@ -592,7 +611,10 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     if ((vstride / 16) % 2 == 0) vstride += 16;
     const size_t per_walker_base =
         (size_t)((c.global_path ? 0 : wstride) + (long long)h->cors.size() * c.n_slices) * h->ft;
-    h->vstride = c.potential_cache == 2 ? 0 : vstride;
+    // the path-shift and single-node moves change slices outside the bisection's
+    // bookkeeping, so they go without the potential cache
+    const bool other_moves = (c.moves & (FS_MOVE_PATH_SHIFT | FS_MOVE_SINGLE_NODE)) != 0;
+    h->vstride = (c.potential_cache == 2 || other_moves) ? 0 : vstride;
     size_t per_walker = per_walker_base + (size_t)h->vstride * h->ft;
     const size_t hist_bytes = (size_t)(c.hist_bins > 0 && !h->hists.empty() ? c.hist_bins : 0) * 4;
     if (c.walkers_per_block > 0) {
@@ -776,6 +798,7 @@ extern "C" int fs_create(const fs_config *cfg, const char *potential, const char
     CREATE_TRY(dalloc(h, (void **)&h->d_bins, h->n_bins * 4));
     CREATE_TRY(dalloc(h, (void **)&h->d_hist, h->n_hist * 8));
     CREATE_TRY(dalloc(h, (void **)&h->d_status, 16));
+    if ((c.moves & FS_MOVE_PATH_SHIFT) && !c.compat) CREATE_TRY(dalloc(h, &h->d_shift_old, W * N * h->ft));
     if (c.learned) {
         CREATE_TRY(dalloc(h, &h->d_mlp_frag, (size_t)FS_MLP_FRAG_BYTES));
         CREATE_TRY(dalloc(h, (void **)&h->d_mlp_bias, (size_t)FS_MLP_NBIAS_FLOATS * 4));
@@ -933,10 +956,26 @@ struct FsArgsHost {  // mirrors FsArgs in fs_pimc.cuh
     unsigned long long *hist;
     int *status;
     double opnorm;
+    void *shift_old;
+    unsigned long long step_base;
     const void *mlp_frag;
     const float *mlp_bias;
     float mlp_inv_scale;
 };
+
+extern "C" int fs_get_step_counter(fs_handle *h, uint64_t *steps)
+{
+    if (!h || !steps) return FS_ERR_CONFIG;
+    *steps = h->steps_done;
+    return FS_OK;
+}
+
+extern "C" int fs_set_step_counter(fs_handle *h, uint64_t steps)
+{
+    if (!h) return FS_ERR_CONFIG;
+    h->steps_done = steps;
+    return FS_OK;
+}
 
 extern "C" int fs_set_learned_proposal(fs_handle *h, const void *frag, size_t frag_bytes, const float *bias,
                                        size_t n_bias, double inv_scale)
@@ -972,9 +1011,12 @@ extern "C" int fs_run(fs_handle *h, int32_t n_launches)
     a.mlp_frag = h->d_mlp_frag;
     a.mlp_bias = h->d_mlp_bias;
     a.mlp_inv_scale = (float)h->mlp_inv_scale;
+    a.shift_old = h->d_shift_old;
     void *args[] = {&a};
     CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), FS_ERR_CUDA);
     for (int i = 0; i < n_launches; i++) {
+        a.step_base = h->steps_done;  // copied at launch
+        h->steps_done += (unsigned long long)c.operator_runs * c.metro_steps_per_operator_run;
         if (h->d_snap)
             CUDA_TRY(h, cudaMemcpyAsync(h->d_snap, h->d_seeds, (h->n_threads + 1) * 16, cudaMemcpyDeviceToDevice,
                                         h->stream), FS_ERR_CUDA);

@@ -252,6 +252,117 @@ __device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream 
     return 1;
 }
 
+#ifndef FS_BISECT
+#define FS_BISECT 1
+#endif
+#ifndef FS_PATH_SHIFT
+#define FS_PATH_SHIFT 0
+#endif
+#ifndef FS_SNM
+#define FS_SNM 0
+#endif
+
+#if FS_PATH_SHIFT || FS_SNM
+// kernel.c:245-249: half the squared step over epsilon^2
+__device__ __forceinline__ FT fs_kin(FT a, FT b)
+{
+    const FT d = FS_SUB(a, b);
+    return FS_MUL(FS_MUL((FT)0.5, FS_MUL(d, d)), (FT)FS_EPS_INV2);
+}
+#endif
+
+#if FS_PATH_SHIFT
+// kernel.c:407-473: shift slices left..right (cyclically) of one degree of freedom by
+// offset; returns the change of the kinetic + potential sum.  left == right shifts nothing.
+__device__ __forceinline__ FT fs_shift(FT *P, int degree, FT offset, fs_u32 left, fs_u32 right)
+{
+    if (left == right) return (FT)0;
+    FT kinDiff = (FT)0, potDiff = (FT)0;
+    fs_u32 ll, rr;
+    if (left < right) {
+        ll = left == 0 ? FS_N - 1 : left - 1;
+        rr = right == FS_N - 1 ? 0 : right + 1;
+    } else {
+        ll = left - 1;
+        rr = right + 1;
+    }
+    kinDiff = FS_SUB(kinDiff, fs_kin(FS_AT(P, degree, left), FS_AT(P, degree, ll)));
+    kinDiff = FS_SUB(kinDiff, fs_kin(FS_AT(P, degree, right), FS_AT(P, degree, rr)));
+    // slices left, left+1, ... right (mod N), in the reference's order
+    const fs_u32 count = left < right ? right - left + 1 : FS_N - left + right + 1;
+#pragma unroll 1
+    for (fs_u32 j = 0; j < count; j++) {
+        const fs_u32 i = (left + j) & (FS_N - 1);
+        potDiff = FS_SUB(potDiff, fs_pot(FS_ARGS_AT(P, i)));
+        FS_AT(P, degree, i) = FS_ADD(FS_AT(P, degree, i), offset);
+        potDiff = FS_ADD(potDiff, fs_pot(FS_ARGS_AT(P, i)));
+    }
+    kinDiff = FS_ADD(kinDiff, fs_kin(FS_AT(P, degree, left), FS_AT(P, degree, ll)));
+    kinDiff = FS_ADD(kinDiff, fs_kin(FS_AT(P, degree, right), FS_AT(P, degree, rr)));
+    return FS_ADD(kinDiff, potDiff);
+}
+
+// kernel.c:640-666: one path-shift move of degree k % DOF; saved holds N values of scratch
+__device__ __forceinline__ int fs_path_shift_move(FT *P, unsigned long long k, FsIStream &is, FsUStream &g,
+                                                  FT *saved)
+{
+    const int degree = (int)(k % FS_DOF);
+    const fs_u32 left = fs_offset(is, FS_N);
+    const fs_u32 right = fs_offset(is, FS_N);
+    const FT offset = FS_MUL((FT)FS_PSALPHA, FS_SUB(FS_MUL((FT)2, fs_uniform(g)), (FT)1));
+#if !FS_COMPAT
+#pragma unroll 1
+    for (int i = 0; i < FS_N; i++) saved[i] = FS_AT(P, degree, i);
+#else
+    (void)saved;
+#endif
+    const FT diff = fs_shift(P, degree, offset, left, right);
+    if (FS_EXP(FS_MUL((FT)(-FS_EPS), diff)) < fs_uniform(g)) {
+#if FS_COMPAT
+        // the reference reverts by shifting again by -offset (kernel.c:654-656), which
+        // leaves the rounding of x + offset - offset in the path
+        if (left != right) {
+            const fs_u32 count = left < right ? right - left + 1 : FS_N - left + right + 1;
+#pragma unroll 1
+            for (fs_u32 j = 0; j < count; j++) {
+                const fs_u32 i = (left + j) & (FS_N - 1);
+                FS_AT(P, degree, i) = FS_ADD(FS_AT(P, degree, i), -offset);
+            }
+        }
+#else
+#pragma unroll 1
+        for (int i = 0; i < FS_N; i++) FS_AT(P, degree, i) = saved[i];
+#endif
+        return 0;
+    }
+    return 1;
+}
+#endif
+
+#if FS_SNM
+// kernel.c:668-705: single-node move of node k mod (N * DOF), uniform in +-alpha
+__device__ __forceinline__ int fs_single_node_move(FT *P, unsigned long long k, FsUStream &g)
+{
+    const fs_u32 modPoint = (fs_u32)(k % FS_N);
+    const int degree = (int)((k % ((unsigned long long)FS_N * FS_DOF)) / FS_N);
+    const fs_u32 l = modPoint == 0 ? FS_N - 1 : modPoint - 1;
+    const fs_u32 r = modPoint == FS_N - 1 ? 0 : modPoint + 1;
+    const FT oldX = FS_AT(P, degree, modPoint);
+    const FT xl = FS_AT(P, degree, l), xr = FS_AT(P, degree, r);
+    const FT modX = FS_ADD(oldX, FS_MUL(FS_SUB(FS_MUL((FT)2, fs_uniform(g)), (FT)1), (FT)FS_ALPHA));
+    FT dE = FS_SUB(FS_SUB(FS_ADD(fs_kin(modX, xr), fs_kin(modX, xl)), fs_kin(oldX, xl)), fs_kin(oldX, xr));
+    dE = FS_SUB(dE, fs_pot(FS_ARGS_AT(P, modPoint)));
+    FS_AT(P, degree, modPoint) = modX;
+    dE = FS_ADD(dE, fs_pot(FS_ARGS_AT(P, modPoint)));
+    FS_AT(P, degree, modPoint) = oldX;
+    if (FS_EXP(FS_MUL((FT)(-FS_EPS), dE)) > fs_uniform(g)) {
+        FS_AT(P, degree, modPoint) = modX;
+        return 1;
+    }
+    return 0;
+}
+#endif
+
 struct FsArgs {
     FT *paths;                 // [walkers][DOF][N]
     fs_u32 *accepts;           // [threads]
@@ -266,6 +377,8 @@ struct FsArgs {
     fs_u64 *hist;              // [hist bins]
     int *status;
     double opnorm;
+    FT *shift_old;             // path shift, fixed mode: the shifted row before the move [walkers][N]
+    unsigned long long step_base;  // fixed mode: Metropolis steps of earlier launches
     const uint2 *mlp_frag;     // learned proposal: network fragments and biases
     const float *mlp_bias;
     float mlp_inv_scale;       // features = endpoint coordinates * mlp_inv_scale
@@ -447,6 +560,25 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         for (int run = 0; run < FS_OPRUNS; run++) {
 #pragma unroll 1
             for (int step = 0; step < FS_MSTEPS; step++) {
+#if !FS_PARALLEL && (FS_PATH_SHIFT || FS_SNM)
+                {
+                    // walker-mode moves ahead of the bisection (kernel.c:640-705).  The
+                    // reference's step counter i*mSteps + j restarts every launch; the fixed
+                    // mode continues it across launches.
+#if FS_COMPAT
+                    const unsigned long long k = (unsigned long long)run * FS_MSTEPS + step;
+#else
+                    const unsigned long long k = a.step_base + (unsigned long long)run * FS_MSTEPS + step;
+#endif
+#if FS_PATH_SHIFT
+                    n_acc += (fs_u32)fs_path_shift_move(P, k, is, fs, a.shift_old + (size_t)w * FS_N);
+#endif
+#if FS_SNM
+                    n_acc += (fs_u32)fs_single_node_move(P, k, fs);
+#endif
+                }
+#endif
+#if FS_BISECT
 #if FS_RANLUX
                 if (t == 0) s_off[wl] = fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N);
                 FS_WSYNC();
@@ -491,6 +623,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #else
                 n_acc += (fs_u32)fs_bisect(P, Vc, start, fs, sigma, nullptr, nullptr);
 #endif
+#endif  // FS_BISECT
                 FS_WSYNC();
             }
             // ---- measurement (kernel.c:734-797) ----

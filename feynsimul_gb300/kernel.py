@@ -146,10 +146,9 @@ class PIMCKernel:
                 raise Exception("Shift path not possible when enableParallelizePath is True.")
         if self._enableGlobalOldPath and not self._enableBisection:
             raise Exception("Old Path is not used when bisection is not enabled")
-        if not self._enableBisection or self._enableSingleNodeMove or self._enablePathShift:
-            raise NotImplementedError(
-                "this engine implements the bisection sampler; the single-node and path-shift "
-                "moves (kernel.c:640-705) are not available")
+        if not (self._enableBisection or self._enableSingleNodeMove or self._enablePathShift):
+            raise Exception("at least one of enableBisection, enablePathShift and enableSingleNodeMove "
+                            "must be True")
         if self._operatorRuns is None:
             raise NameError('operatorRuns need to be set.')
         if self._metroStepsPerOperatorRun is None:
@@ -172,7 +171,7 @@ class PIMCKernel:
         c = FsConfig()
         c.dof = self._system.DOF
         c.n_slices = self._N
-        c.bisection_level = self._S
+        c.bisection_level = self._S if self._S is not None else 1
         c.beta = self._beta
         c.n_walkers = self._nbrOfWalkers
         c.walkers_per_group = self._nbrOfWalkersPerWorkGroup if self._enableParallelizePath else 1
@@ -199,6 +198,12 @@ class PIMCKernel:
         c.global_path = int(bool(self._enableGlobalPath)) if self._enableBisection else 0
         pc = getattr(ka, "potentialCache", None)
         c.potential_cache = 0 if pc is None else (1 if pc else 2)
+        c.moves = ((_lib.FS_MOVE_BISECTION if self._enableBisection else 0)
+                   | (_lib.FS_MOVE_PATH_SHIFT if self._enablePathShift else 0)
+                   | (_lib.FS_MOVE_SINGLE_NODE if self._enableSingleNodeMove else 0))
+        c.alpha = float(ka.alpha) if self._enableSingleNodeMove else 0.0
+        c.ps_alpha = float(getattr(ka, "PSAlpha", None) or 0.0) if self._enablePathShift else 0.0
+        self._movesPerStep = bin(c.moves).count("1")
         self._learned = bool(c.learned)
         self._cfg = c
 
@@ -503,8 +508,12 @@ class PIMCKernel:
         return out
 
     def getAcceptanceRate(self):
-        """Mean acceptance rate of the last run (kernel.py:648-658)."""
-        return (self.getAccepts() / float(self._operatorRuns * self._metroStepsPerOperatorRun)).mean()
+        """Mean acceptance rate of the last run (kernel.py:648-658).  The reference divides
+        every move type's accepts by the steps alone (so walker mode with several move
+        types can exceed 1); reference-compatible mode repeats that, otherwise the rate is
+        per move."""
+        moves = 1 if self._compat else self._movesPerStep
+        return (self.getAccepts() / float(self._operatorRuns * self._metroStepsPerOperatorRun * moves)).mean()
 
     def getSeeds(self):
         out = np.empty((self._nbrOfThreads + 1, 4), np.uint32)
@@ -572,8 +581,10 @@ class PIMCKernel:
         and the run counter.  restoreState() on a kernel built from the same KernelArgs
         continues bit for bit as if the run had not stopped."""
         L = lib()
+        steps = ctypes.c_uint64()
+        check(L.fs_get_step_counter(self._handle, ctypes.byref(steps)), self._handle)
         st = {"paths": self.getPaths(), "runs_since_zero": np.array(self._runsSinceZero),
-              "fingerprint": np.array(self._config_fingerprint())}
+              "fingerprint": np.array(self._config_fingerprint()), "step_counter": np.array(steps.value, np.uint64)}
         if self._enableRanlux:
             st["ranlux_tab"], st["group_tab"] = self.getRanluxTables()
         else:
@@ -611,6 +622,8 @@ class PIMCKernel:
             h = np.ascontiguousarray(st["histogram"], dtype=np.uint64)
             check(L.fs_set_histogram(self._handle, h.ctypes.data, h.size), self._handle)
         self._runsSinceZero = int(st["runs_since_zero"])
+        if "step_counter" in st:
+            check(L.fs_set_step_counter(self._handle, int(st["step_counter"])), self._handle)
 
     def saveCheckpoint(self, filename):
         np.savez(filename, **self.getState())

@@ -107,7 +107,17 @@ typedef struct fs_config {
      * potential only at its proposed nodes): 0 = automatic, 1 = on, 2 = off.  Results are
      * bit-identical either way; it trades shared memory (occupancy) for potential work. */
     int32_t potential_cache;
+    /* Move types per Metropolis step, walker mode (enable_parallelize_path = 0) for all but
+     * the bisection: 0 = bisection only (the default); otherwise a mask of FS_MOVE_* --
+     * enableBisection / enablePathShift / enableSingleNodeMove (kernel.py:68-73,
+     * :192-198, kernel.c:640-705).  Per step the path shift comes first, then the
+     * single-node move, then the bisection. */
+    int32_t moves;
+    double alpha;     /* single-node move width: node += alpha * (2u - 1) (kernel_args.py:124-126) */
+    double ps_alpha;  /* path-shift width: offset = PSAlpha * (2u - 1) (kernel_args.py:128-131) */
 } fs_config;
+
+enum { FS_MOVE_BISECTION = 1, FS_MOVE_PATH_SHIFT = 2, FS_MOVE_SINGLE_NODE = 4 };
 
 /* fs_query output */
 typedef struct fs_info {
@@ -201,6 +211,11 @@ int fs_reduce_correlator(fs_handle *h, int64_t walker_begin, int64_t walker_end,
  * the path precision): walker w gets template w % n_template, replicated on the device.
  * For walker counts whose full path array is impractical to stage in host memory. */
 int fs_set_paths_tiled(fs_handle *h, const void *host, size_t n_template);
+/* Metropolis steps of all launches so far (operator_runs * metro_steps_per_operator_run
+ * per launch); the fixed mode's single-node and path-shift moves continue their node /
+ * degree counter from it.  Set it when restoring a checkpoint. */
+int fs_get_step_counter(fs_handle *h, uint64_t *steps);
+int fs_set_step_counter(fs_handle *h, uint64_t steps);
 /* device time of the last fs_run call (all its launches), seconds */
 int fs_get_run_time(fs_handle *h, double *seconds);
 

@@ -146,6 +146,10 @@ def capture(ka_kwargs: dict, system, np_seed: int):
     """Run the reference's PIMCKernel.__init__ under the stub; return what it produced."""
     rk, rka = reference_modules()
     ka = rka.KernelArgs(system=system, **ka_kwargs)
+    # kernel_args.py takes PSAlpha (:41) but never stores it, and kernel.py:127 reads
+    # ka.PSAlpha: set the attribute as a caller of the reference has to
+    if "PSAlpha" in ka_kwargs and not hasattr(ka, "PSAlpha"):
+        ka.PSAlpha = ka_kwargs["PSAlpha"]
     np.random.seed(np_seed)
     with _int_sizes_randint():
         k = rk.PIMCKernel(ka)

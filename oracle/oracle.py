@@ -62,6 +62,11 @@ class OracleConfig:
     xMin: float = 0.0
     xMax: float = 1.0
     binResolutionPerDOF: int = 1
+    enableBisection: bool = True
+    enablePathShift: bool = False       # walker mode only (kernel.py:192-198)
+    enableSingleNodeMove: bool = False
+    alpha: float = 0.0                  # single-node move width (kernel_args.py:124-126)
+    PSAlpha: float = 0.0                # path-shift width (kernel_args.py:128-131)
     # additions of this project (same meaning as in the CUDA kernels)
     compat: bool = False
     accum: int = 1                      # 0 ref FP32, 1 FP64, 2 Kahan, 3 study
@@ -107,6 +112,10 @@ def _defines(c: OracleConfig) -> str:
         "FS_OPNORM": "%1.17e" % c.opnorm,
         "FS_BINS": int(bool(c.enableBins)),
         "FS_NHIST": len(c.histograms) if c.histBins > 0 else 0,
+        "FS_BISECT": int(bool(c.enableBisection)),
+        "FS_PATH_SHIFT": int(bool(c.enablePathShift)), "FS_SNM": int(bool(c.enableSingleNodeMove)),
+        "FS_EPS_INV2": "%1.17e" % ((float(c.N) / c.beta) ** 2),
+        "FS_ALPHA": "%1.17e" % c.alpha, "FS_PSALPHA": "%1.17e" % c.PSAlpha,
     }
     if c.enableBins:
         d.update({"FS_XMIN": "%1.17e" % c.xMin, "FS_XMAX": "%1.17e" % c.xMax,
@@ -169,7 +178,8 @@ class _Args(ctypes.Structure):
                 ("paths", "accepts", "seeds", "walker_seeds", "ranlux_tab", "group_tab",
                  "op_means", "cor_means", "bins", "hist")] + \
                [("walker_begin", ctypes.c_int), ("walker_end", ctypes.c_int),
-                ("omp_threads", ctypes.c_int), ("opnorm", ctypes.c_double)]
+                ("omp_threads", ctypes.c_int), ("opnorm", ctypes.c_double),
+                ("step_base", ctypes.c_ulonglong)]
 
 
 def _ptr(a):
@@ -204,6 +214,7 @@ class OracleSampler:
         self.cor_means = np.zeros((W, max(len(c.correlators), 1), c.N // 2), cor_ft)
         self.bins = np.zeros(c.binResolutionPerDOF ** c.DOF if c.enableBins else 1, np.uint32)
         self.hist = np.zeros(max(c.histBins, 1), np.uint64)
+        self.launches = 0
 
     def init_ranlux_rows(self, table: np.ndarray, xs):
         xs = np.ascontiguousarray(np.asarray(xs, dtype=np.uint64))
@@ -222,9 +233,11 @@ class OracleSampler:
         a.walker_end = c.nbrOfWalkers if walker_end is None else walker_end
         a.omp_threads = self.omp_threads or os.cpu_count() or 1
         a.opnorm = c.opnorm
+        a.step_base = self.launches * c.operatorRuns * c.metroStepsPerOperatorRun
         rc = self.lib.fso_run(ctypes.byref(a))
         if rc != 0:
             raise RuntimeError(f"oracle run failed ({rc})")
+        self.launches += 1
 
 
 # ---- stand-alone RNG streams (no plugin needed) -------------------------------------

@@ -150,6 +150,80 @@ static int fso_bisect(FT *path, uint32_t start, fso_stream_t *g, const FT *sigma
     return 1;
 }
 
+#ifndef FS_BISECT
+#define FS_BISECT 1
+#endif
+#ifndef FS_PATH_SHIFT
+#define FS_PATH_SHIFT 0
+#endif
+#ifndef FS_SNM
+#define FS_SNM 0
+#endif
+
+#if FS_PATH_SHIFT || FS_SNM
+/* kernel.c:245-249: half the squared step over epsilon^2 */
+static inline FT fso_kin(FT a, FT b)
+{
+    FT d = a - b;
+    return (FT)0.5 * (d * d) * (FT)FS_EPS_INV2;
+}
+#endif
+
+#if FS_PATH_SHIFT
+/* kernel.c:407-473: shift slices left..right (cyclically) of one degree of freedom by
+ * offset and return the change of the kinetic + potential sum.  left == right shifts
+ * nothing. */
+static FT fso_shift(FT *path, int degree, FT offset, uint32_t left, uint32_t right)
+{
+    if (left == right) return 0.0;
+    FT kinDiff = 0.0, potDiff = 0.0;
+    FT *x = path + (size_t)degree * FS_N;
+    if (left < right) {
+        uint32_t rr = right + 1, ll = left - 1;
+        if (left == 0) ll = FS_N - 1;
+        if (right == FS_N - 1) rr = 0;
+        kinDiff -= fso_kin(x[left], x[ll]);
+        kinDiff -= fso_kin(x[right], x[rr]);
+        for (uint32_t i = left; i <= right; i++) {
+            potDiff -= fs_pot(FS_ARGS_AT(path, i));
+            x[i] = x[i] + offset;
+            potDiff += fs_pot(FS_ARGS_AT(path, i));
+        }
+        kinDiff += fso_kin(x[left], x[ll]);
+        kinDiff += fso_kin(x[right], x[rr]);
+    } else {
+        kinDiff -= fso_kin(x[left], x[left - 1]);
+        kinDiff -= fso_kin(x[right], x[right + 1]);
+        for (uint32_t i = left; i < FS_N; i++) {
+            potDiff -= fs_pot(FS_ARGS_AT(path, i));
+            x[i] += offset;
+            potDiff += fs_pot(FS_ARGS_AT(path, i));
+        }
+        for (uint32_t i = 0; i <= right; i++) {
+            potDiff -= fs_pot(FS_ARGS_AT(path, i));
+            x[i] += offset;
+            potDiff += fs_pot(FS_ARGS_AT(path, i));
+        }
+        kinDiff += fso_kin(x[left], x[left - 1]);
+        kinDiff += fso_kin(x[right], x[right + 1]);
+    }
+    return kinDiff + potDiff;
+}
+
+/* the reference's revert (kernel.c:654-656): the same shift by -offset */
+static void fso_shift_back(FT *path, int degree, FT offset, uint32_t left, uint32_t right)
+{
+    if (left == right) return;
+    FT *x = path + (size_t)degree * FS_N;
+    if (left < right) {
+        for (uint32_t i = left; i <= right; i++) x[i] = x[i] + -offset;
+    } else {
+        for (uint32_t i = left; i < FS_N; i++) x[i] += -offset;
+        for (uint32_t i = 0; i <= right; i++) x[i] += -offset;
+    }
+}
+#endif
+
 typedef struct {
     FT *paths;               /* [walkers][DOF][N] */
     uint32_t *accepts;       /* [threads] */
@@ -163,6 +237,7 @@ typedef struct {
     unsigned long long *hist;/* [nbins] */
     int walker_begin, walker_end, omp_threads;
     double opnorm;           /* 1 / (operatorRuns * slices per thread), as a double */
+    unsigned long long step_base; /* fixed mode: Metropolis steps of earlier launches */
 } fso_args_t;
 
 /* reference thread id of segment t of walker w (kernel.c:539-541) */
@@ -312,8 +387,61 @@ int fso_run(fso_args_t *A)
                     acc[t] += (uint32_t)fso_bisect(path, start, &fs[t], sigma);
                 }
 #else
+                /* kernel.c:640-705: the step counter i*mSteps + j restarts every launch in
+                 * the reference; the fixed mode continues it across launches */
+#if FS_COMPAT
+                const unsigned long long k = (unsigned long long)run * FS_MSTEPS + step;
+#else
+                const unsigned long long k = A->step_base + (unsigned long long)run * FS_MSTEPS + step;
+#endif
+                (void)k;
+#if FS_PATH_SHIFT
+                {
+                    const int degree = (int)(k % FS_DOF);
+                    const uint32_t left = fso_offset(&is, FS_N);
+                    const uint32_t right = fso_offset(&is, FS_N);
+                    const FT offset = (FT)FS_PSALPHA * ((FT)2.0 * fso_uniform(&fs[0]) - (FT)1.0);
+#if !FS_COMPAT
+                    FT saved[FS_N];
+                    memcpy(saved, path + (size_t)degree * FS_N, sizeof(saved));
+#endif
+                    const FT diff = fso_shift(path, degree, offset, left, right);
+                    if (exp(-(FT)FS_EPS * diff) < fso_uniform(&fs[0])) {
+#if FS_COMPAT
+                        fso_shift_back(path, degree, offset, left, right);
+#else
+                        memcpy(path + (size_t)degree * FS_N, saved, sizeof(saved));
+#endif
+                    } else {
+                        acc[0]++;
+                    }
+                }
+#endif
+#if FS_SNM
+                {
+                    const uint32_t modPoint = (uint32_t)(k % FS_N);
+                    const uint32_t modPathPoint = (uint32_t)(k % ((unsigned long long)FS_N * FS_DOF));
+                    uint32_t ri = modPathPoint + 1, li = modPathPoint - 1;
+                    if (modPoint == 0) li += FS_N;
+                    else if (modPoint == FS_N - 1) ri -= FS_N;
+                    const FT oldX = path[modPathPoint];
+                    const FT modX = oldX + ((FT)2.0 * fso_uniform(&fs[0]) - (FT)1.0) * (FT)FS_ALPHA;
+                    FT diffE = fso_kin(modX, path[ri]) + fso_kin(modX, path[li]) - fso_kin(path[modPathPoint], path[li]) -
+                               fso_kin(path[modPathPoint], path[ri]);
+                    diffE -= fs_pot(FS_ARGS_AT(path, modPoint));
+                    path[modPathPoint] = modX;
+                    diffE += fs_pot(FS_ARGS_AT(path, modPoint));
+                    path[modPathPoint] = oldX;
+                    if (exp(-(FT)FS_EPS * diffE) > fso_uniform(&fs[0])) {
+                        path[modPathPoint] = modX;
+                        acc[0]++;
+                    }
+                }
+#endif
+#if FS_BISECT
                 uint32_t start = fso_offset(&is, FS_N) % FS_N;
                 acc[0] += (uint32_t)fso_bisect(path, start, &fs[0], sigma);
+#endif
 #endif
             }
             /* measurement, kernel.c:734-797 */

@@ -55,6 +55,17 @@ CASES = {
                                nbrOfWalkers=4, S=3),
     "xorshift_parallel_s1_big": dict(BASE, nbrOfWalkers=4, N=64, S=1, nbrOfWalkersPerWorkGroup=4,
                                      operatorRuns=2, metroStepsPerOperatorRun=3),
+    # walker-mode move types (kernel.c:407-473, :640-705)
+    "xorshift_walker_moves": dict(BASE, enableParallelizePath=False, nbrOfWalkersPerWorkGroup=1,
+                                  enablePathShift=True, PSAlpha=0.7, enableSingleNodeMove=True, alpha=0.9,
+                                  metroStepsPerOperatorRun=7),
+    "xorshift_walker_snm_only": dict(BASE, enableParallelizePath=False, nbrOfWalkersPerWorkGroup=1,
+                                     enableBisection=False, enableSingleNodeMove=True, alpha=1.2),
+    "ranlux_walker_moves": dict(BASE, enableRanlux=True, luxuaryFactor=1, ranluxIntMax=2 ** 32 - 1,
+                                enableParallelizePath=False, nbrOfWalkersPerWorkGroup=1, nbrOfWalkers=4,
+                                enablePathShift=True, PSAlpha=0.5, enableSingleNodeMove=True, alpha=0.7),
+    "xorshift_walker_shift_double": dict(BASE, enableParallelizePath=False, nbrOfWalkersPerWorkGroup=1,
+                                         enableDouble=True, enablePathShift=True, PSAlpha=0.6),
 }
 
 
@@ -128,7 +139,10 @@ def main():
         raise SystemExit("reference tree not present; fixtures are generated where it is")
     make_ranlux()
     make_lm2m2()
+    only = sys.argv[1:]
     for name, ka in CASES.items():
+        if only and name not in only:
+            continue
         make_sweep(name, ka)
         print("wrote", name)
 

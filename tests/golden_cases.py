@@ -40,4 +40,7 @@ def oracle_config(ka, compat=True, accum=0):
         operators=tuple(ka["operators"]) if ka["enableOperator"] else (),
         correlators=tuple(ka["correlators"]) if ka["enableCorrelator"] else (),
         enableBins=ka["enableBins"], xMin=ka["xMin"], xMax=ka["xMax"],
-        binResolutionPerDOF=ka["binResolutionPerDOF"], compat=compat, accum=accum)
+        binResolutionPerDOF=ka["binResolutionPerDOF"], compat=compat, accum=accum,
+        enableBisection=ka.get("enableBisection", True), enablePathShift=ka.get("enablePathShift", False),
+        enableSingleNodeMove=ka.get("enableSingleNodeMove", False), alpha=ka.get("alpha") or 0.0,
+        PSAlpha=ka.get("PSAlpha") or 0.0)

@@ -98,6 +98,10 @@ FIXED_CASES = {
     "ranlux_parallel_lux2": dict(nbrOfWalkers=8, nbrOfWalkersPerWorkGroup=2),
     "ranlux_walker_lux0": {},
     "xorshift_parallel_double": {},
+    "xorshift_walker_moves": {},
+    "xorshift_walker_snm_only": {},
+    "ranlux_walker_moves": {},
+    "xorshift_walker_shift_double": {},
 }
 
 

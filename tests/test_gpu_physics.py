@@ -111,3 +111,62 @@ def test_modn_short_run(tmp_path):
     assert e8 < e32 < 0.55
     outdir = tsv[0].rsplit("/", 1)[0]
     assert glob.glob(outdir + "/pathsN32episode*") and glob.glob(outdir + "/checkpoint.npz")
+
+
+def _ho_walker_kernel(moves, walkers=2048, N=16, beta=4.0, op_runs=50, msteps=4, seed=9):
+    kernel, kernel_args = engine()
+    sysm = types.SimpleNamespace(DOF=1, potential="0.5 * 1.0 * x1 * x1", userCode="")
+    ka = kernel_args.KernelArgs(
+        system=sysm, nbrOfWalkers=walkers, N=N, beta=beta, S=2, enableOperator=True, enableCorrelator=False,
+        enableBisection="bisection" in moves, enablePathShift="shift" in moves,
+        enableSingleNodeMove="single" in moves, alpha=0.8, PSAlpha=0.5, enableBins=False,
+        nbrOfWalkersPerWorkGroup=1, enableParallelizePath=False, enableGlobalPath=False,
+        enableGlobalOldPath=False, operators=("1.0 * x1 * x1",), operatorRuns=op_runs,
+        metroStepsPerOperatorRun=msteps, seed=seed)
+    return kernel.PIMCKernel(ka)
+
+
+@pytest.mark.parametrize("moves", [("single",), ("shift", "single"), ("shift", "bisection")])
+def test_ho_walker_moves_match_exact_values(moves):
+    """Single-node and path-shift moves (kernel.c:640-705) sample the exact discretised HO.
+    The fixed mode carries the single-node counter across launches, so every node moves."""
+    require_gpu()
+    N, beta = 16, 4.0
+    k = _ho_walker_kernel(moves, N=N, beta=beta)
+    for _ in range(10):
+        k.run()
+    e = []
+    for _ in range(30):
+        k.run()
+        e.append(k.getOperators()[0].mean())
+    e = np.array(e)
+    x2, _ = exact_ho(beta, N, [0])
+    tau_guard = 3.0  # launches are correlated for local moves: widen the error bar
+    se = e.std(ddof=1) / np.sqrt(len(e)) * tau_guard
+    assert abs(e.mean() - x2) < 5 * se + 2e-3, (e.mean(), x2, se)
+    assert 0.1 < k.getAcceptanceRate() < 1.0
+    k.close()
+
+
+def test_walker_moves_checkpoint_resume_is_bit_identical(tmp_path):
+    """Resuming restores the move counter too: the continued run equals the unbroken one."""
+    require_gpu()
+    mv = ("shift", "single", "bisection")
+    a = _ho_walker_kernel(mv, walkers=128, op_runs=3, msteps=5)
+    for _ in range(4):
+        a.run()
+    b = _ho_walker_kernel(mv, walkers=128, op_runs=3, msteps=5)
+    for _ in range(2):
+        b.run()
+    b.saveCheckpoint(str(tmp_path / "ck.npz"))
+    b.close()
+    c = _ho_walker_kernel(mv, walkers=128, op_runs=3, msteps=5)
+    c.loadCheckpoint(str(tmp_path / "ck.npz"))
+    for _ in range(2):
+        c.run()
+    sa, sc = a.getState(), c.getState()
+    for key in ("paths", "seeds", "walker_seeds", "step_counter"):
+        assert np.array_equal(sa[key], sc[key]), key
+    np.testing.assert_array_equal(a.getAccepts(), c.getAccepts())
+    a.close()
+    c.close()
