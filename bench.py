@@ -253,13 +253,21 @@ def alg_ops_per_node(config, ka):
     return rng + bm + 2 * POT_OPS[config]
 
 
-def roofline_for(config, ka, node_rate, clk):
+# DRAM bytes per fs_metropolis launch from one ncu capture of the default workload
+# (dram__bytes_read.sum + dram__bytes_write.sum; profiles/fs_metropolis_he3_lm2m2_ranlux.md)
+TRAFFIC_PER_LAUNCH = {"he3": 226.3e6}
+
+
+def roofline_for(config, ka, node_rate, clk, default_workload=True):
     sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
     peak = 4 * 32 * 152 * sm_mhz * 1e6 / 1e12            # Tera lane-ops/s
     per_node = alg_ops_per_node(config, ka)
     achieved = node_rate * per_node / 1e12
+    traffic = TRAFFIC_PER_LAUNCH.get(config) if default_workload else None
     return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
-            "frac": achieved / peak, "traffic": None,
+            "frac": achieved / peak, "traffic": traffic,
+            "traffic_unit": "DRAM bytes per launch (ncu), against the ~250 MB of paths, RANLUX tables and "
+                            "results a launch must move: the kernel is not memory bound",
             "alg_ops_per_node": per_node,
             "peak_basis": f"4 x 32 x 152 lanes per clock at the sampled median SM clock {sm_mhz:.0f} MHz "
                           "(MEASURED_PEAKS.json has HBM and bf16 peaks only; this kernel uses neither)"}
@@ -398,26 +406,26 @@ def run_gb300(args, rank, world):
     value = nodes * args.steps * world / t_dev
     ms_per_step = 1e3 * t_dev / args.steps
 
-    # ---- end to end through the reference-facing API, host buffers ----
-    cudart = torch.cuda.cudart()
+    # ---- end to end through the public API, host buffers ----
+    # Each step: this step's input paths copied in from pinned host memory, the sweeps, the
+    # paths copied back (PIMCKernel.runHost: chunks of walkers pipelined over three
+    # streams), and the per-walker operator means read back and reduced on the host.
     host_paths = np.ascontiguousarray(k.getPaths())
     try:
-        cudart.cudaHostRegister(host_paths.ctypes.data, host_paths.nbytes, 0)
+        k.pinHost(host_paths)
         pinned = True
     except Exception:
         pinned = False
     energies = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        k.setPaths(host_paths)          # H2D: this step's input paths
-        k.run()
+        k.runHost(host_paths, out=host_paths, chunks=args.chunks)
         ops = k.getOperators()          # D2H: per-thread operator means, reduced per walker
-        k.getPaths(out=host_paths)      # D2H: the paths the next step starts from
         energies.append(ops[0])
     t_e2e = time.perf_counter() - t0
     if pinned:
         try:
-            cudart.cudaHostUnregister(host_paths.ctypes.data)
+            k.unpinHost(host_paths)
         except Exception:
             pass
     e2e_value = nodes * args.steps * world / t_e2e
@@ -431,7 +439,8 @@ def run_gb300(args, rank, world):
     ess_per_s = ess / (ms_per_step * 1e-3 * args.steps)
 
     # ---- roofline: the sweep is bound by instruction issue (see roofline_for) ----
-    roof = roofline_for(args.config, ka, value / world, clk)
+    roof = roofline_for(args.config, ka, value / world, clk,
+                        default_workload=not (args.walkers or args.op_runs or args.msteps))
 
     result = {
         "metric": "path-node updates/s (plain Metropolis-bisection sampler)",
@@ -444,11 +453,12 @@ def run_gb300(args, rank, world):
                    "parallelism": f"replicas x{world}", "walkers_per_block": int(info.walkers_per_block),
                    "registers": int(info.registers), "smem_bytes": int(info.smem_bytes)},
         "e2e": {"value": e2e_value, "unit": "node-updates/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "pinned": pinned},
+                "d2h_bytes_per_step": int(d2h), "pinned": pinned, "api": "PIMCKernel.runHost + getOperators",
+                "chunks": args.chunks},
         "energy_ess_per_s": ess_per_s, "energy_tau_int_runs": tau,
         "energy_mean": float(series[series.shape[0] // 2:].mean()),
         "acceptance_rate": float(k.getAcceptanceRate()),
-        "gpu_launches": args.steps * 2,
+        "gpu_launches": args.steps * (1 + args.chunks),
         "roofline": roof, "clocks": clk,
     }
     k.close()
@@ -470,6 +480,7 @@ def main():
     ap.add_argument("--msteps", type=int, default=0, help="override metroStepsPerOperatorRun")
     ap.add_argument("--wpb", type=int, default=0, help="walkers per thread block (0 = automatic)")
     ap.add_argument("--minb", type=int, default=-1, help="thread blocks per SM to compile for (-1 = tuned default)")
+    ap.add_argument("--chunks", type=int, default=4, help="walker chunks pipelined in the e2e step (1 = no overlap)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

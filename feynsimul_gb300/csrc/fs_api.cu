@@ -79,6 +79,10 @@ struct fs_handle {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t k_metro = nullptr, k_rinit = nullptr;
     cudaStream_t stream = nullptr;
+    cudaStream_t s_in = nullptr, s_out = nullptr;  // fs_run_host copy streams
+    cudaStream_t s_comp2 = nullptr;                 // fs_run_host: second compute stream
+    double *d_wops = nullptr;                       // fs_get_walker_operators output
+    std::vector<cudaEvent_t> ev_chunk;               // fs_run_host: copy-in / compute done per chunk
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
     // device buffers
@@ -554,7 +558,7 @@ static void free_buffers(fs_handle *h)
 {
     void *bufs[] = {h->d_paths, h->d_accepts, h->d_seeds, h->d_snap, h->d_wseeds, h->d_rtab,
                     h->d_gtab, h->d_bins, h->d_ops, h->d_cor, h->d_hist, h->d_status,
-                    h->d_mlp_frag, h->d_mlp_bias, h->d_red, h->d_shift_old};
+                    h->d_mlp_frag, h->d_mlp_bias, h->d_red, h->d_shift_old, h->d_wops};
     for (void *p : bufs)
         if (p) cudaFree(p);
 }
@@ -817,6 +821,10 @@ extern "C" int fs_destroy(fs_handle *h)
     free_buffers(h);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    for (cudaEvent_t e : h->ev_chunk) cudaEventDestroy(e);
+    if (h->s_in) cudaStreamDestroy(h->s_in);
+    if (h->s_out) cudaStreamDestroy(h->s_out);
+    if (h->s_comp2) cudaStreamDestroy(h->s_comp2);
     if (h->lib) cudaLibraryUnload(h->lib);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -961,6 +969,7 @@ struct FsArgsHost {  // mirrors FsArgs in fs_pimc.cuh
     const void *mlp_frag;
     const float *mlp_bias;
     float mlp_inv_scale;
+    int block_offset;
 };
 
 extern "C" int fs_get_step_counter(fs_handle *h, uint64_t *steps)
@@ -988,6 +997,8 @@ extern "C" int fs_set_learned_proposal(fs_handle *h, const void *frag, size_t fr
     return rc;
 }
 
+static void fill_args(fs_handle *h, FsArgsHost &a);
+
 extern "C" int fs_run(fs_handle *h, int32_t n_launches)
 {
     if (!h) return FS_ERR_CONFIG;
@@ -995,6 +1006,121 @@ extern "C" int fs_run(fs_handle *h, int32_t n_launches)
     const fs_config &c = h->cfg;
     CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
     FsArgsHost a;
+    fill_args(h, a);
+    void *args[] = {&a};
+    CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), FS_ERR_CUDA);
+    for (int i = 0; i < n_launches; i++) {
+        a.step_base = h->steps_done;  // copied at launch
+        h->steps_done += (unsigned long long)c.operator_runs * c.metro_steps_per_operator_run;
+        if (h->d_snap)
+            CUDA_TRY(h, cudaMemcpyAsync(h->d_snap, h->d_seeds, (h->n_threads + 1) * 16, cudaMemcpyDeviceToDevice,
+                                        h->stream), FS_ERR_CUDA);
+        CUDA_TRY(h, cudaLaunchKernel((const void *)h->k_metro, dim3(h->grid), dim3(h->block), args, h->smem, h->stream),
+                 FS_ERR_LAUNCH);
+    }
+    CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), FS_ERR_CUDA);
+    h->timed = true;
+    return FS_OK;
+}
+
+// Pipelined run on host path buffers: the walkers are split into n_chunks CTA-aligned
+// chunks; chunk c's paths are copied in on one stream, its n_launches sweeps run on the
+// handle's stream as soon as they have arrived, and its paths are copied out on a third
+// stream while later chunks compute.  Walkers are independent, so this equals
+// set_paths + run + get_paths bit for bit (the reference-compatible xorshift mode, whose
+// walker streams read other walkers' seed rows, runs as one chunk).
+extern "C" int fs_run_host(fs_handle *h, const void *paths_in, void *paths_out, int32_t n_launches,
+                           int32_t n_chunks)
+{
+    if (!h || !paths_in || !paths_out) return FS_ERR_CONFIG;
+    if (n_launches < 1 || n_chunks < 1) return fail(h, FS_ERR_CONFIG, "n_launches and n_chunks must be >= 1");
+    const fs_config &c = h->cfg;
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    if (h->d_snap) n_chunks = 1;
+    n_chunks = std::min(n_chunks, std::min(h->grid, 64));
+    if (!h->s_in) CUDA_TRY(h, cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking), FS_ERR_CUDA);
+    if (!h->s_out) CUDA_TRY(h, cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking), FS_ERR_CUDA);
+    if (!h->s_comp2) CUDA_TRY(h, cudaStreamCreateWithFlags(&h->s_comp2, cudaStreamNonBlocking), FS_ERR_CUDA);
+    while ((int)h->ev_chunk.size() < 2 * n_chunks + 2) {
+        cudaEvent_t e;
+        CUDA_TRY(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), FS_ERR_CUDA);
+        h->ev_chunk.push_back(e);
+    }
+    FsArgsHost a;
+    fill_args(h, a);
+    void *args[] = {&a};
+    const size_t bpw = (size_t)c.dof * c.n_slices * h->ft;
+    const unsigned long long per_launch = (unsigned long long)c.operator_runs * c.metro_steps_per_operator_run;
+    CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), FS_ERR_CUDA);
+    // the copy streams start after everything queued before this call
+    CUDA_TRY(h, cudaStreamWaitEvent(h->s_in, h->ev0, 0), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamWaitEvent(h->s_out, h->ev0, 0), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamWaitEvent(h->s_comp2, h->ev0, 0), FS_ERR_CUDA);
+    // chunks alternate between two compute streams, so one chunk's last wave overlaps the
+    // next chunk's first (they touch disjoint walkers; shared histograms use atomics)
+    cudaStream_t comp[2] = {h->stream, h->s_comp2};
+    for (int k = 0; k < n_chunks; k++) {
+        const int cta0 = (int)((long long)h->grid * k / n_chunks);
+        const int cta1 = (int)((long long)h->grid * (k + 1) / n_chunks);
+        const size_t w0 = (size_t)cta0 * h->wpb;
+        const size_t w1 = std::min((size_t)cta1 * h->wpb, (size_t)c.n_walkers);
+        if (cta1 <= cta0 || w1 <= w0) continue;
+        cudaEvent_t e_in = h->ev_chunk[2 * k], e_done = h->ev_chunk[2 * k + 1];
+        CUDA_TRY(h, cudaMemcpyAsync((char *)h->d_paths + w0 * bpw, (const char *)paths_in + w0 * bpw, (w1 - w0) * bpw,
+                                    cudaMemcpyHostToDevice, h->s_in), FS_ERR_CUDA);
+        CUDA_TRY(h, cudaEventRecord(e_in, h->s_in), FS_ERR_CUDA);
+        cudaStream_t cs = comp[k & 1];
+        CUDA_TRY(h, cudaStreamWaitEvent(cs, e_in, 0), FS_ERR_CUDA);
+        a.block_offset = cta0;
+        for (int i = 0; i < n_launches; i++) {
+            a.step_base = h->steps_done + per_launch * (unsigned long long)i;
+            if (h->d_snap)
+                CUDA_TRY(h, cudaMemcpyAsync(h->d_snap, h->d_seeds, (h->n_threads + 1) * 16, cudaMemcpyDeviceToDevice,
+                                            cs), FS_ERR_CUDA);
+            CUDA_TRY(h, cudaLaunchKernel((const void *)h->k_metro, dim3(cta1 - cta0), dim3(h->block), args, h->smem,
+                                         cs), FS_ERR_LAUNCH);
+        }
+        CUDA_TRY(h, cudaEventRecord(e_done, cs), FS_ERR_CUDA);
+        CUDA_TRY(h, cudaStreamWaitEvent(h->s_out, e_done, 0), FS_ERR_CUDA);
+        CUDA_TRY(h, cudaMemcpyAsync((char *)paths_out + w0 * bpw, (const char *)h->d_paths + w0 * bpw, (w1 - w0) * bpw,
+                                    cudaMemcpyDeviceToHost, h->s_out), FS_ERR_CUDA);
+    }
+    h->steps_done += per_launch * (unsigned long long)n_launches;
+    // the handle's stream (fs_sync, the getters) waits for the second compute stream and
+    // the last copy out
+    cudaEvent_t e_end = h->ev_chunk[2 * n_chunks], e_c2 = h->ev_chunk[2 * n_chunks + 1];
+    CUDA_TRY(h, cudaEventRecord(e_end, h->s_out), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaEventRecord(e_c2, h->s_comp2), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamWaitEvent(h->stream, e_end, 0), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamWaitEvent(h->stream, e_c2, 0), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), FS_ERR_CUDA);
+    h->timed = true;
+    return FS_OK;
+}
+
+extern "C" int fs_pin_host(void *ptr, size_t bytes)
+{
+    cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(nullptr, FS_ERR_CUDA, "cudaHostRegister: %s", cudaGetErrorString(e));
+    }
+    return FS_OK;
+}
+
+extern "C" int fs_unpin_host(void *ptr)
+{
+    cudaError_t e = cudaHostUnregister(ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(nullptr, FS_ERR_CUDA, "cudaHostUnregister: %s", cudaGetErrorString(e));
+    }
+    return FS_OK;
+}
+
+static void fill_args(fs_handle *h, FsArgsHost &a)
+{
+    const fs_config &c = h->cfg;
     a.paths = h->d_paths;
     a.accepts = h->d_accepts;
     a.seeds = h->d_seeds;
@@ -1012,20 +1138,8 @@ extern "C" int fs_run(fs_handle *h, int32_t n_launches)
     a.mlp_bias = h->d_mlp_bias;
     a.mlp_inv_scale = (float)h->mlp_inv_scale;
     a.shift_old = h->d_shift_old;
-    void *args[] = {&a};
-    CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), FS_ERR_CUDA);
-    for (int i = 0; i < n_launches; i++) {
-        a.step_base = h->steps_done;  // copied at launch
-        h->steps_done += (unsigned long long)c.operator_runs * c.metro_steps_per_operator_run;
-        if (h->d_snap)
-            CUDA_TRY(h, cudaMemcpyAsync(h->d_snap, h->d_seeds, (h->n_threads + 1) * 16, cudaMemcpyDeviceToDevice,
-                                        h->stream), FS_ERR_CUDA);
-        CUDA_TRY(h, cudaLaunchKernel((const void *)h->k_metro, dim3(h->grid), dim3(h->block), args, h->smem, h->stream),
-                 FS_ERR_LAUNCH);
-    }
-    CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), FS_ERR_CUDA);
-    h->timed = true;
-    return FS_OK;
+    a.step_base = h->steps_done;
+    a.block_offset = 0;
 }
 
 extern "C" int fs_sync(fs_handle *h)
@@ -1080,6 +1194,48 @@ extern "C" int fs_get_operators(fs_handle *h, double *out, size_t n)
     if (rc) return rc;
     if (h->op_elem == 4) widen<float>(raw, out, n);
     else widen<double>(raw, out, n);
+    return FS_OK;
+}
+
+// per-walker operator means: the mean over the walker's own threads of their per-thread
+// means (thread ids as in the sweep, kernel.c:539-541), FP64, out[op][walker]
+template <class T>
+__global__ void fs_walker_ops_kernel(const T *ops, int n_walkers, int tpw, int wpg, int nwg, int nops, int parallel,
+                                     double *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_walkers * nops) return;
+    const int op = i / n_walkers, w = i - op * n_walkers;
+    double s = 0.0;
+    for (int t = 0; t < tpw; t++) {
+        const long long tid = parallel ? (long long)(w / wpg) * tpw + t + (long long)(w % wpg) * nwg * tpw : w;
+        s += (double)ops[tid * nops + op];
+    }
+    out[(size_t)op * n_walkers + w] = s / tpw;
+}
+
+extern "C" int fs_get_walker_operators(fs_handle *h, double *out, size_t n)
+{
+    if (!h || !out) return FS_ERR_CONFIG;
+    const fs_config &c = h->cfg;
+    const int nops = (int)h->ops.size();
+    if (n != (size_t)nops * c.n_walkers) return fail(h, FS_ERR_IO, "expected %zu values", (size_t)nops * c.n_walkers);
+    if (c.accum == 3) return fail(h, FS_ERR_STATE, "study accumulation keeps three columns: use fs_get_operators");
+    if (nops == 0) return FS_OK;
+    CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    if (!h->d_wops) CUDA_TRY(h, cudaMalloc((void **)&h->d_wops, n * sizeof(double)), FS_ERR_OOM);
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    const int par = c.enable_parallelize_path ? 1 : 0;
+    const int nwg = c.n_walkers / std::max(1, c.walkers_per_group);
+    if (h->op_elem == 8)
+        fs_walker_ops_kernel<double><<<grid, 256, 0, h->stream>>>((const double *)h->d_ops, c.n_walkers, h->tpw,
+                                                                  c.walkers_per_group, nwg, nops, par, h->d_wops);
+    else
+        fs_walker_ops_kernel<float><<<grid, 256, 0, h->stream>>>((const float *)h->d_ops, c.n_walkers, h->tpw,
+                                                                 c.walkers_per_group, nwg, nops, par, h->d_wops);
+    CUDA_TRY(h, cudaGetLastError(), FS_ERR_LAUNCH);
+    CUDA_TRY(h, cudaMemcpyAsync(out, h->d_wops, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
     return FS_OK;
 }
 

@@ -382,6 +382,7 @@ struct FsArgs {
     const uint2 *mlp_frag;     // learned proposal: network fragments and biases
     const float *mlp_bias;
     float mlp_inv_scale;       // features = endpoint coordinates * mlp_inv_scale
+    int block_offset;          // first CTA of this launch (chunked launches of fs_run_host)
 };
 
 __device__ __forceinline__ int fs_thread_id(int w, int t)
@@ -439,7 +440,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     const int tid_b = threadIdx.x;
     const int wl = tid_b / FS_TPW;
     const int t = tid_b % FS_TPW;
-    const int w0 = blockIdx.x * FS_WPB;
+    const int w0 = (blockIdx.x + a.block_offset) * FS_WPB;
     const int w = w0 + wl;
     const int n_here = min(FS_WPB, FS_NWALKERS - w0);
     const bool active = wl < n_here;

@@ -270,6 +270,34 @@ class PIMCKernel:
         if wait:
             self.sync()
 
+    def runHost(self, paths, out=None, launches=1, chunks=4):
+        """setPaths(paths) + run(launches) + getPaths(out) as one pipelined call: the walkers
+        are split into ``chunks`` chunks whose host-to-device copy, sweeps and copy back
+        overlap (fs_run_host).  Same results bit for bit.  The copies overlap only when
+        ``paths`` and ``out`` are page-locked (``pinHost``).  Returns ``out``."""
+        a = np.asarray(paths)
+        n = self._nbrOfWalkers * self._N * self._system.DOF
+        if a.dtype != self._ftype or not a.flags["C_CONTIGUOUS"] or a.size != n:
+            raise ValueError("paths must be a C-contiguous array of the paths' size and dtype")
+        if out is None:
+            out = np.empty((self._nbrOfWalkers, self._N * self._system.DOF), self._ftype)
+        elif out.dtype != self._ftype or not out.flags["C_CONTIGUOUS"] or out.size != n:
+            raise ValueError("out must be a C-contiguous array of the paths' size and dtype")
+        check(lib().fs_run_host(self._handle, a.ctypes.data, out.ctypes.data, int(launches), int(chunks)),
+              self._handle)
+        self._runsSinceZero += int(launches)
+        self.sync()
+        return out
+
+    @staticmethod
+    def pinHost(array):
+        """Page-lock a numpy array's memory for overlapped copies (undo with unpinHost)."""
+        check(lib().fs_pin_host(array.ctypes.data, array.nbytes))
+
+    @staticmethod
+    def unpinHost(array):
+        check(lib().fs_unpin_host(array.ctypes.data))
+
     def _thread_rows_compat_group(self):
         """Group-seed index of every thread: group + lid1 * nWG (kernel.c:165)."""
         T, WPG, nWG = self._threadsPerWalker, self._nbrOfWalkersPerWorkGroup, self._nbrOfWorkgroups
@@ -364,6 +392,11 @@ class PIMCKernel:
             raise Exception("Can only return operator when created with"
                             "kernelArg.enableOperator = True")
         nops = len(self._operators)
+        if not self._compat and self._accumulation != "study":
+            # the walkers' own thread means, averaged on the device
+            out = np.empty((nops, self._nbrOfWalkers), np.float64)
+            check(lib().fs_get_walker_operators(self._handle, out.ctypes.data, out.size), self._handle)
+            return out
         raw = self._raw_operators()
         if self._accumulation == "study":
             raw = raw.reshape(-1, 3)[:, 2]

@@ -181,6 +181,16 @@ int fs_set_ranlux_tables(fs_handle *h, const uint32_t *tab, size_t n_tab_rows,
 /* One reference run() = operator_runs x metro_steps_per_operator_run sweeps, launched
  * n_launches times back to back.  Asynchronous. */
 int fs_run(fs_handle *h, int32_t n_launches);
+/* n_launches runs on host path buffers ([walkers][DOF][N] in the path precision; in and
+ * out may be the same buffer), pipelined: the walkers are split into n_chunks chunks whose
+ * copy-in, sweeps and copy-out overlap on three streams.  Equivalent to fs_set_paths +
+ * fs_run + fs_get_paths (kernel.py:567-574, :459-506, :557-565); asynchronous like fs_run
+ * (the buffers must stay valid until fs_sync), and overlapping only for page-locked host
+ * memory (fs_pin_host). */
+int fs_run_host(fs_handle *h, const void *paths_in, void *paths_out, int32_t n_launches, int32_t n_chunks);
+/* page-lock / release a host buffer (cudaHostRegister) for overlapped copies */
+int fs_pin_host(void *ptr, size_t bytes);
+int fs_unpin_host(void *ptr);
 int fs_sync(fs_handle *h);
 int fs_sync_timeout(fs_handle *h, double seconds);
 
@@ -192,6 +202,10 @@ int fs_sync_timeout(fs_handle *h, double seconds);
  * Kahan compensation, FP64 sum.  Bins: [res^DOF] counts.  Histogram: [hist_bins] counts. */
 int fs_get_operators(fs_handle *h, double *out, size_t n);
 int fs_get_correlator(fs_handle *h, double *out, size_t n);
+/* Per-walker operator means [n_ops][walkers]: each walker's thread means averaged on the
+ * device in FP64 (the fixed-mode reduction of PIMCKernel.getOperators, kernel.py:576-606).
+ * Not for FS_ACCUM_STUDY. */
+int fs_get_walker_operators(fs_handle *h, double *out, size_t n);
 int fs_get_accepts(fs_handle *h, uint32_t *out, size_t n);
 int fs_get_bins(fs_handle *h, uint32_t *out, size_t n);
 int fs_get_histogram(fs_handle *h, uint64_t *out, size_t n);

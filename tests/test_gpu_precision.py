@@ -101,8 +101,10 @@ def test_fp64_everywhere_matches_oracle():
 def test_study_columns_and_device_moments():
     sysm = _cluster(4)
     W, N, S = 96, 64, 2
-    ks = _kernel(sysm, W, N, S, True, accumulation="study", fast=True)
-    kd = _kernel(sysm, W, N, S, True, accumulation="fp64", fast=True)
+    # IEEE builds: with FMA contraction allowed, two differently generated modules may
+    # round the operator expression differently
+    ks = _kernel(sysm, W, N, S, True, accumulation="study", fast=False)
+    kd = _kernel(sysm, W, N, S, True, accumulation="fp64", fast=False)
     p0 = sysm.initial_paths(W, N, np.random.RandomState(4)).astype(np.float32)
     for k in (ks, kd):
         k.setPaths(p0)
@@ -117,7 +119,7 @@ def test_study_columns_and_device_moments():
     np.testing.assert_allclose(raw[:, 0], raw[:, 3], rtol=1e-4)
     np.testing.assert_allclose(raw[:, 1], raw[:, 3], rtol=1e-5)
     st = ks.getOperatorsStudy()
-    np.testing.assert_array_equal(st[2], kd.getOperators())
+    np.testing.assert_allclose(st[2], kd.getOperators(), rtol=1e-14)  # host vs device mean
     np.testing.assert_allclose(st[0], st[2], rtol=1e-5)
     # device moments vs the host reduction of the per-walker values
     per = ks.getCorrelatorStudy()                       # (3, W, 1, N/2)
