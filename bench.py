@@ -368,10 +368,12 @@ def run_gb300(args, rank, world):
     sysm, ka, extra, workload = setup(**workload_overrides(args))
     minb = args.minb if args.minb >= 0 else TUNED_MIN_BLOCKS.get(args.config, 0)
     wpb = args.wpb if args.wpb > 0 else TUNED_WPB.get(args.config, 0)
-    ka_obj = KernelArgs(system=sysm, seed=1000 + rank, walkersPerBlock=wpb,
+    from feynsimul_gb300.replicas import ReplicaGroup, replica_seed
+    group = ReplicaGroup()
+    ka_obj = KernelArgs(system=sysm, seed=replica_seed(1000, rank), walkersPerBlock=wpb,
                         minBlocksPerSM=minb, **extra, **ka)
     k = PIMCKernel(ka_obj)
-    paths0 = initial_paths(sysm, ka, 17 + rank)
+    paths0 = initial_paths(sysm, ka, replica_seed(17, rank))
     k.setPaths(paths0)
     if ka["enableRanlux"]:
         k.initRanlux()
@@ -397,12 +399,7 @@ def run_gb300(args, rank, world):
         times.append(k.getRunTime())
     torch.cuda.synchronize()
     clk = clocks.stop()
-    t_dev = float(np.sum(times))
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt.item())
+    t_dev = group.max(float(np.sum(times)))
     value = nodes * args.steps * world / t_dev
     ms_per_step = 1e3 * t_dev / args.steps
 
@@ -417,12 +414,15 @@ def run_gb300(args, rank, world):
     except Exception:
         pinned = False
     energies = []
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         k.runHost(host_paths, out=host_paths, chunks=args.chunks)
         ops = k.getOperators()          # D2H: per-thread operator means, reduced per walker
         energies.append(ops[0])
-    t_e2e = time.perf_counter() - t0
+    t_e2e = group.max(time.perf_counter() - t0)
     if pinned:
         try:
             k.unpinHost(host_paths)
@@ -457,6 +457,7 @@ def run_gb300(args, rank, world):
                 "chunks": args.chunks},
         "energy_ess_per_s": ess_per_s, "energy_tau_int_runs": tau,
         "energy_mean": float(series[series.shape[0] // 2:].mean()),
+        "energy_all_replicas": group.merge(series[series.shape[0] // 2:].mean(axis=0)),
         "acceptance_rate": float(k.getAcceptanceRate()),
         "gpu_launches": args.steps * (1 + args.chunks),
         "roofline": roof, "clocks": clk,
