@@ -289,14 +289,73 @@ def learned_study(quick=True):
                     S_plain=(4, 5) if quick else (3, 4, 5, 6), S_learned=(4, 5) if quick else (4, 5, 6, 7),
                     launches=40 if quick else 60, train_steps=1500 if quick else 3000,
                     kernel_extra=dict(enableRanlux=True, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
-                                      minBlocksPerSM=3), log=lambda *a: None)
+                                      walkersPerBlock=TUNED_WPB["he3"], minBlocksPerSM=TUNED_MIN_BLOCKS["he3"]),
+                    log=lambda *a: None)
     out = {"metric": "energy ESS/s, learned vs plain sampler (He3 LM2M2 T=1K N=256 16384 walkers RANLUX)",
            "summary": res["summary"], "wall_s": time.perf_counter() - t0,
            "plain": {str(k): {kk: v[kk] for kk in ("acceptance", "tau_int_launches", "ess_per_s",
                                                     "node_updates_per_s")} for k, v in res["plain"].items()},
            "learned": {str(k): {kk: v[kk] for kk in ("acceptance", "tau_int_launches", "ess_per_s",
-                                                      "node_updates_per_s", "loss_start", "loss_end")}
+                                                      "node_updates_per_s", "loss_start", "loss_end",
+                                                      "validation_gain_nats", "fallback")}
                        for k, v in res["learned"].items()}}
+    if not quick:
+        out["coarse_ho"] = coarse_ho_gain()
+    return out
+
+
+def coarse_ho_gain(N=32, S=3, beta=16.0, walkers=4096, seed=3):
+    """Where the free bridge is poor -- the HO with eps = 0.5 and 8-slice segments spanning
+    4 time units -- the trained network's acceptance and energy ESS per sweep against the
+    plain sampler's, from the same starting paths."""
+    import types
+    from feynsimul_gb300.kernel import PIMCKernel
+    from feynsimul_gb300.kernel_args import KernelArgs
+    from feynsimul_gb300.learned import LearnedProposal, harvest_triples, sigma_level
+    from feynsimul_gb300.stats import ess
+    sysm = types.SimpleNamespace(DOF=1, potential="0.5 * 1.0 * x1 * x1", userCode="")
+
+    def make(learned, sd):
+        return PIMCKernel(KernelArgs(
+            system=sysm, nbrOfWalkers=walkers, N=N, beta=beta, S=S, enableOperator=True,
+            enableCorrelator=False, enableBisection=True, enablePathShift=False, enableSingleNodeMove=False,
+            enableBins=False, nbrOfWalkersPerWorkGroup=1, enableParallelizePath=True, enableGlobalPath=False,
+            enableGlobalOldPath=False, operators=("1.0 * x1 * x1",), operatorRuns=1, metroStepsPerOperatorRun=1,
+            seed=sd, learnedProposal=learned))
+    plain = make(False, seed)
+    for _ in range(200):
+        plain.run()
+    s1 = sigma_level(beta, N, S, 1)
+    feats, z = [], []
+    for _ in range(8):
+        for _ in range(10):
+            plain.run()
+        f, t = harvest_triples(plain.getPaths(), 1, N, S, s1, 1.0)
+        feats.append(f)
+        z.append(t)
+    feats, z = np.concatenate(feats), np.concatenate(z)
+    n_val = feats.shape[0] // 10
+    model = LearnedProposal(1, s1, 1.0, seed=seed)
+    model.train(feats[n_val:], z[n_val:], steps=1500, batch=4096, lr=2e-3, seed=seed)
+    start = plain.getPaths()
+    lrn = make(True, seed + 1)
+    lrn.setLearnedProposal(model)
+    out = {"workload": f"HO beta={beta} N={N} S={S} {walkers} walkers, one sweep per measurement",
+           "validation_gain_nats": model.validation_gain(feats[:n_val], z[:n_val])}
+    for name, k in (("plain", plain), ("learned", lrn)):
+        k.setPaths(start)
+        series, ar, t = [], [], 0.0
+        for _ in range(300):
+            k.run()
+            t += k.getRunTime()
+            ar.append(k.getAcceptanceRate())
+            series.append(k.getOperators()[0])
+        e, tau = ess(np.array(series))
+        out[name] = {"acceptance": float(np.mean(ar)), "tau_int_sweeps": float(tau), "ess_per_sweep_per_walker":
+                     float(e / (300 * walkers)), "ess_per_s": float(e / t)}
+        k.close()
+    out["ess_per_sweep_gain"] = out["learned"]["ess_per_sweep_per_walker"] / out["plain"]["ess_per_sweep_per_walker"]
+    out["ess_per_s_gain"] = out["learned"]["ess_per_s"] / out["plain"]["ess_per_s"]
     return out
 
 

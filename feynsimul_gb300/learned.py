@@ -179,6 +179,16 @@ class LearnedProposal:
         s = 4.0 * np.tanh(0.25 * y[:, self.dof:2 * self.dof])
         return o, np.exp(0.5 * s)
 
+    def validation_gain(self, feats, targets):
+        """Held-out log-likelihood gain over the free-particle bridge, in nats per segment:
+        the free proposal's negative log-likelihood (mean 0, width sigma_1) minus the
+        network's, averaged over (feats, targets).  Positive means the network proposes the
+        level-1 midpoint better than the plain bisection."""
+        o, sd = self.conditional(feats)
+        z = np.asarray(targets, np.float64)[:, :self.dof]
+        nll = 0.5 * ((z - o) / sd) ** 2 + np.log(sd)
+        return float(np.mean(np.sum(0.5 * z * z - nll, axis=1)))
+
     # ---- training on the GPU with the project's kernels ----
     def train(self, feats, targets, steps=2000, batch=4096, lr=1e-3, seed=0, log_every=0):
         """Adam on the Gaussian negative log-likelihood; returns the loss history (per step,
@@ -239,10 +249,15 @@ def energy_series(kernel, launches, op_index=0):
 
 def ess_study(system, beta, N, walkers, S_plain=(3, 4, 5, 6), S_learned=(4, 5, 6, 7), launches=60,
               op_runs=1, msteps=4, burn=10, train_steps=3000, harvest_snapshots=4, seed=1,
-              kernel_extra=None, log=print):
+              kernel_extra=None, min_gain=0.01, log=print):
     """Energy-estimator ESS/s of the plain sampler and of the learned proposal on one
     system.  Every sampler starts from the same equilibrated paths; a launch is op_runs x
-    msteps sweeps followed by one operator measurement per walker and run."""
+    msteps sweeps followed by one operator measurement per walker and run.
+
+    The learned sampler keeps the plain bisection as its fallback: a network whose held-out
+    log-likelihood gain over the free bridge (LearnedProposal.validation_gain, on 10% of the
+    harvested segments) is below ``min_gain`` nats per segment is not used, and that level
+    runs the plain kernel (reported with ``fallback: True``)."""
     from .kernel import PIMCKernel
     from .kernel_args import KernelArgs
     from .stats import ess, tau_int_batch_means
@@ -306,22 +321,39 @@ def ess_study(system, beta, N, walkers, S_plain=(3, 4, 5, 6), S_learned=(4, 5, 6
             feats.append(f)
             z.append(t)
         feats, z = np.concatenate(feats), np.concatenate(z)
+        n_val = max(1, feats.shape[0] // 10)
         model = LearnedProposal(system.DOF, s1, length_scale, seed=seed)
-        hist = model.train(feats, z, steps=train_steps, batch=8192, lr=1e-3, seed=seed)
-        k = make(S, True)
-        k.setLearnedProposal(model)
-        r = measure(k, "learned")
-        r.update(train_samples=int(feats.shape[0]), loss_start=float(hist[:20].mean()),
-                 loss_end=float(hist[-50:].mean()))
+        hist = model.train(feats[n_val:], z[n_val:], steps=train_steps, batch=8192, lr=1e-3, seed=seed)
+        gain = model.validation_gain(feats[:n_val], z[:n_val])
+        info = dict(train_samples=int(feats.shape[0] - n_val), loss_start=float(hist[:20].mean()),
+                    loss_end=float(hist[-50:].mean()), validation_gain_nats=gain)
+        if gain < min_gain:
+            if S not in results["plain"]:
+                k = make(S, False)
+                results["plain"][S] = measure(k, "plain  ")
+                k.close()
+            r = dict(results["plain"][S], fallback=True, **info)
+            log(f"learned S={S}: validation gain {gain:.4f} nats < {min_gain}: plain bisection (fallback)")
+        else:
+            k = make(S, True)
+            k.setLearnedProposal(model)
+            r = measure(k, "learned")
+            r.update(fallback=False, **info)
+            k.close()
         results["learned"][S] = r
-        k.close()
     best_plain = max(results["plain"].values(), key=lambda r: r["ess_per_s"])
     best_learned = max(results["learned"].values(), key=lambda r: r["ess_per_s"])
+    used = [r for r in results["learned"].values() if not r["fallback"]]
+    best_net = max(used, key=lambda r: r["ess_per_s"]) if used else None
     ref = results["plain"].get(4, best_plain)
     results["summary"] = {
         "plain_S4_ess_per_s": ref["ess_per_s"], "best_plain_S": best_plain["S"],
         "best_plain_ess_per_s": best_plain["ess_per_s"], "best_learned_S": best_learned["S"],
         "best_learned_ess_per_s": best_learned["ess_per_s"],
+        "best_learned_is_fallback": bool(best_learned["fallback"]),
         "learned_vs_plain_S4": best_learned["ess_per_s"] / ref["ess_per_s"],
-        "learned_vs_best_plain": best_learned["ess_per_s"] / best_plain["ess_per_s"]}
+        "learned_vs_best_plain": best_learned["ess_per_s"] / best_plain["ess_per_s"],
+        "network_levels_used": sorted(int(r["S"]) for r in used),
+        "network_only_vs_best_plain": (best_net["ess_per_s"] / best_plain["ess_per_s"]) if best_net else None,
+        "validation_gain_nats": {int(S): r["validation_gain_nats"] for S, r in results["learned"].items()}}
     return results

@@ -190,3 +190,49 @@ def test_training_recovers_ho_conditional():
     sd_exact = np.sqrt(var) / s1
     assert np.all(np.abs(o[:, 0] - o_exact) < 0.06 + 0.05 * np.abs(o_exact)), (o[:, 0], o_exact)
     assert np.all(np.abs(sd[:, 0] - sd_exact) < 0.05 * sd_exact), (sd[:, 0], sd_exact)
+
+
+def test_trained_network_gains_where_the_free_bridge_is_poor():
+    """Coarse slicing (eps = 0.5, 8-slice segments spanning 4 time units of the HO): the
+    free-particle midpoint is far from the exact conditional.  The trained proposal raises
+    the acceptance of the same moves and the sampled <x^2> stays exact."""
+    from feynsimul_gb300.learned import LearnedProposal, harvest_triples, sigma_level
+    N, S, beta = 32, 3, 16.0
+    walkers = 4096
+    plain = _ho_kernel(False, N=N, S=S, beta=beta, walkers=walkers, op_runs=10, msteps=2)
+    for _ in range(10):
+        plain.run()
+    s1 = sigma_level(beta, N, S, 1)
+    feats, z = [], []
+    for _ in range(6):
+        plain.run()
+        f, t = harvest_triples(plain.getPaths(), 1, N, S, s1, 1.0)
+        feats.append(f)
+        z.append(t)
+    start = plain.getPaths()
+    feats, z = np.concatenate(feats), np.concatenate(z)
+    n_val = feats.shape[0] // 10
+    model = LearnedProposal(1, s1, 1.0)
+    assert abs(model.validation_gain(feats[:n_val], z[:n_val])) < 1e-6  # untrained: the free bridge
+    model.train(feats[n_val:], z[n_val:], steps=1500, batch=4096, lr=2e-3)
+    assert model.validation_gain(feats[:n_val], z[:n_val]) > 0.01
+    lrn = _ho_kernel(True, N=N, S=S, beta=beta, walkers=walkers, op_runs=10, msteps=2, seed=12)
+    lrn.setLearnedProposal(model)
+    acc = {}
+    e = {}
+    for name, k in (("plain", plain), ("learned", lrn)):
+        k.setPaths(start)
+        ar, en = [], []
+        for _ in range(15):
+            k.run()
+            ar.append(k.getAcceptanceRate())
+            en.append(k.getOperators()[0].mean())
+        acc[name] = float(np.mean(ar))
+        e[name] = np.array(en)
+    x2, _, _ = _exact_ho(beta, N, S)
+    se = e["learned"].std(ddof=1) / np.sqrt(len(e["learned"]))
+    assert abs(e["learned"].mean() - x2) < 5 * se + 2e-3, (e["learned"].mean(), x2, se)
+    print("acceptance", acc, "x2", {k: float(v.mean()) for k, v in e.items()}, "exact", x2)
+    assert acc["learned"] > acc["plain"] + 0.05, acc
+    plain.close()
+    lrn.close()
