@@ -366,7 +366,7 @@ def batch_bench(args):
     from feynsimul_gb300 import build as fb
     fb.build()
     from feynsimul_gb300.batch import BatchSampler, autotune, ragged_workload
-    wl = ragged_workload(seed=0, n_systems=64)
+    wl = ragged_workload(seed=0, n_systems=args.systems)
     t0 = time.perf_counter()
     tune = autotune(wl, op_runs=1, msteps=4)
     t_tune = time.perf_counter() - t0
@@ -376,6 +376,16 @@ def batch_bench(args):
     steps = max(3, min(args.steps, 10))
     t = b.run(steps, graph=True)
     value = b.node_updates_per_launch * steps / t
+    # algorithmic lane operations of one launch: per system, node updates x (xorshift 8 per
+    # uniform x 2 DOF uniforms + Box-Muller 9 per DOF + two LM2M2 cluster evaluations)
+    ops = 0.0
+    for w, sy in zip(wl, b.systems):
+        n, dof = w["n"], 3 * (w["n"] - 1)
+        nodes = w["walkers"] * (w["N"] >> sy.bisection_level) * ((1 << sy.bisection_level) - 1) * 4
+        ops += nodes * (16 * dof + 9 * dof + 2 * lm2m2_cluster_ops(n))
+    clk_mhz = 2070.0
+    peak = 4 * 32 * 152 * clk_mhz * 1e6 / 1e12
+    achieved = ops * steps / t / 1e12
     out = {"metric": "path-node updates/s, ragged batch of 64 LM2M2 systems in one persistent launch",
            "value": value, "unit": "node-updates/s", "n_gpus": 1, "steps": steps, "warmup": max(3, args.warmup),
            "ms_per_step": 1e3 * t / steps, "higher_is_better": True, "dtype": "f32 (u32 RNG, f64 sums)",
@@ -388,9 +398,20 @@ def batch_bench(args):
            "autotune": {"cached": tune["cached"], "seconds": t_tune,
                         "candidates": [{k: c.get(k) for k in ("block_threads", "tpw_target", "node_updates_per_s",
                                                               "error")} for c in tune.get("candidates", [])]},
-           "gpu_launches": steps}
+           "gpu_launches": steps,
+           "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
+                        "frac": achieved / peak, "traffic": None,
+                        "alg_ops_per_node": ops / b.node_updates_per_launch,
+                        "peak_basis": "4 x 32 x 152 lanes per clock at 2070 MHz"}}
     b.close()
     return out
+
+
+def lm2m2_cluster_ops(n):
+    """Lane operations of one LM2M2 cluster potential evaluation: the positions from the
+    Jacobi coordinates (3n(n-1) multiply-adds) and per pair 6 for r^2 and ~40 for the pair
+    potential (rsqrt, dispersion polynomial, two exponentials, the add-on cosine, selects)."""
+    return 3 * n * (n - 1) + 46 * n * (n - 1) // 2
 
 
 # ------------------------------------------------------------------ arms
@@ -408,7 +429,14 @@ def precision_bench(args):
     if args.msteps:
         kw["msteps"] = args.msteps
     r = precision_study(launches=max(2, args.steps), log=lambda m: print(m, file=sys.stderr), **kw)
-    return {"metric": "precision study: FP32-path error vs FP64-everywhere, per result",
+    dof = 27
+    per_node = 16 * dof + 9 * dof + 2 * lm2m2_cluster_ops(10)
+    peak = 4 * 32 * 152 * 2070.0 * 1e6 / 1e12
+    achieved = r["fp32_node_updates_per_s"] * per_node / 1e12
+    return {"roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
+                         "frac": achieved / peak, "traffic": None, "alg_ops_per_node": per_node,
+                         "peak_basis": "4 x 32 x 152 lanes per clock at 2070 MHz (FP32 arm)"},
+            "metric": "precision study: FP32-path error vs FP64-everywhere, per result",
             "value": r["fp32_node_updates_per_s"], "unit": "node-updates/s (FP32 path, study sums)",
             "n_gpus": 1, "higher_is_better": True, "dtype": "f32 path, f64/f32/kahan sums",
             "data": "synthetic, seeded", "config": {"workload": r["workload"]}, "study": r}
@@ -513,12 +541,12 @@ def run_gb300(args, rank, world):
                    "registers": int(info.registers), "smem_bytes": int(info.smem_bytes)},
         "e2e": {"value": e2e_value, "unit": "node-updates/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "pinned": pinned, "api": "PIMCKernel.runHost + getOperators",
-                "chunks": args.chunks},
+                "chunks": k.lastChunks},
         "energy_ess_per_s": ess_per_s, "energy_tau_int_runs": tau,
         "energy_mean": float(series[series.shape[0] // 2:].mean()),
         "energy_all_replicas": group.merge(series[series.shape[0] // 2:].mean(axis=0)),
         "acceptance_rate": float(k.getAcceptanceRate()),
-        "gpu_launches": args.steps * (1 + args.chunks),
+        "gpu_launches": args.steps * (1 + k.lastChunks),
         "roofline": roof, "clocks": clk,
     }
     k.close()
@@ -540,7 +568,9 @@ def main():
     ap.add_argument("--msteps", type=int, default=0, help="override metroStepsPerOperatorRun")
     ap.add_argument("--wpb", type=int, default=0, help="walkers per thread block (0 = automatic)")
     ap.add_argument("--minb", type=int, default=-1, help="thread blocks per SM to compile for (-1 = tuned default)")
-    ap.add_argument("--chunks", type=int, default=4, help="walker chunks pipelined in the e2e step (1 = no overlap)")
+    ap.add_argument("--chunks", type=int, default=0,
+                    help="walker chunks pipelined in the e2e step (0 = automatic, 1 = no overlap)")
+    ap.add_argument("--systems", type=int, default=64, help="batch config: number of systems (small profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -37,7 +37,7 @@ EXPORTS = (
     "fs_batch_run", "fs_batch_sync", "fs_batch_get_run_time", "fs_batch_set_paths", "fs_batch_get_paths",
     "fs_batch_set_seeds", "fs_batch_get_op_sums", "fs_batch_get_accepts", "fs_batch_query",
     "fs_reduce_correlator", "fs_set_paths_tiled", "fs_get_step_counter", "fs_set_step_counter",
-    "fs_run_host", "fs_pin_host", "fs_unpin_host", "fs_get_walker_operators",
+    "fs_run_host", "fs_pin_host", "fs_unpin_host", "fs_get_walker_operators", "fs_get_last_chunks",
 )
 
 FS_MOVE_BISECTION, FS_MOVE_PATH_SHIFT, FS_MOVE_SINGLE_NODE = 1, 2, 4
@@ -117,6 +117,7 @@ _PROTOS = {
     "fs_get_step_counter": ([_P, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
     "fs_run_host": ([_P, _P, _P, _I, _I], ctypes.c_int),
     "fs_get_walker_operators": ([_P, _P, _S], ctypes.c_int),
+    "fs_get_last_chunks": ([_P, ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
     "fs_pin_host": ([_P, _S], ctypes.c_int),
     "fs_unpin_host": ([_P], ctypes.c_int),
     "fs_set_step_counter": ([_P, ctypes.c_uint64], ctypes.c_int),

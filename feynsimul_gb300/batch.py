@@ -39,9 +39,20 @@ def ragged_workload(seed=0, n_systems=64, n_range=(3, 10), N_choices=(128, 256, 
     return out
 
 
-def choose_S(N, tpw_target, block):
+def choose_S(N, tpw_target, block, dof=None, smem_budget=200 * 1024):
+    """Bisection level of one system: N / 2^S = tpw_target segment threads per walker, except
+    where a walker's path fills most of a tile's shared memory (large clusters): then the
+    walker gets up to the whole CTA (segments of at least 8 slices), so the tile does not
+    leave most of its warps idle."""
     S = int(np.log2(N)) - int(np.log2(tpw_target))
     S = max(1, min(S, 10, int(np.log2(N))))
+    if dof is not None:
+        walker_bytes = dof * (N + N // 8) * 4 + 512
+        wpb_max = max(1, smem_budget // walker_bytes)
+        if wpb_max * (N >> S) < block and N >= 8:
+            tpw = 1 << int(np.log2(max(1, block // wpb_max)))
+            tpw = min(tpw, N // 8)
+            S = min(S, max(1, int(np.log2(N // tpw))))
     while (N >> S) > block:
         S += 1
     return S
@@ -62,7 +73,7 @@ class BatchSampler:
         self.systems = []
         for w in workload:
             c = clusters[w["n"]]
-            S = choose_S(w["N"], tpw_target, block_threads)
+            S = choose_S(w["N"], tpw_target, block_threads, dof=c.DOF)
             self.systems.append(FsBatchSystem(type=self.type_of[w["n"]], n_walkers=w["walkers"], n_slices=w["N"],
                                               bisection_level=S, beta=1.0 / w["T"], walkers_per_tile=0))
         arr = (FsBatchSystem * len(self.systems))(*self.systems)
@@ -140,8 +151,13 @@ class BatchSampler:
         return out
 
 
+# bumped when the batch kernel or its launch-shape rules change, so cached tunings expire
+_TUNING_VERSION = 2
+
+
 def _signature(workload, op_runs, msteps):
-    return hashlib.sha1(json.dumps([workload, op_runs, msteps], sort_keys=True).encode()).hexdigest()[:16]
+    return hashlib.sha1(json.dumps([workload, op_runs, msteps, _TUNING_VERSION],
+                                   sort_keys=True).encode()).hexdigest()[:16]
 
 
 def autotune(workload, op_runs=1, msteps=4, candidates=None, cache_file=None, launches=2, log=None):

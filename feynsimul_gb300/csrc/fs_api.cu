@@ -75,6 +75,7 @@ struct fs_handle {
     double *d_red = nullptr;  // fs_reduce_correlator output (sum, sumsq)
     void *d_shift_old = nullptr;  // path shift, fixed mode: row saved before the move
     unsigned long long steps_done = 0;  // Metropolis steps of all launches so far
+    int last_chunks = 0;                // chunks (kernel launches per sweep set) of the last fs_run_host
     // CUDA objects
     cudaLibrary_t lib = nullptr;
     cudaKernel_t k_metro = nullptr, k_rinit = nullptr;
@@ -352,11 +353,16 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
         at << (i ? ", " : "") << "FS_AT(P, " << i << ", (i))";
     }
     o << "#define FS_ARGS_AT(P, i) " << at.str() << "\n";
-    o << "__device__ __forceinline__ FT fs_pot(" << args.str() << ") { return (" << cvt(potential)
+    // Plugins of more than 8 DOF (clusters of 4+ atoms, tens of pair terms) are called, not
+    // inlined: the sweep evaluates the potential at several places, and inlined copies of a
+    // 45-pair potential overflow the instruction cache (measured: +19% to +47% on a 10-atom
+    // cluster).
+    const char *inl = c.dof > 8 ? "__device__ __noinline__ " : "__device__ __forceinline__ ";
+    o << inl << "FT fs_pot(" << args.str() << ") { return (" << cvt(potential)
       << "); }\n";
     auto fn = [&](const char *name, const std::vector<std::string> &ex) {
         if (ex.empty()) return;
-        o << "__device__ __forceinline__ void " << name << "(" << args.str() << ", FT *o) {\n";
+        o << inl << "void " << name << "(" << args.str() << ", FT *o) {\n";
         for (size_t i = 0; i < ex.size(); i++) o << "    o[" << i << "] = (" << cvt(ex[i]) << ");\n";
         o << "}\n";
     };
@@ -1033,11 +1039,23 @@ extern "C" int fs_run_host(fs_handle *h, const void *paths_in, void *paths_out, 
                            int32_t n_chunks)
 {
     if (!h || !paths_in || !paths_out) return FS_ERR_CONFIG;
-    if (n_launches < 1 || n_chunks < 1) return fail(h, FS_ERR_CONFIG, "n_launches and n_chunks must be >= 1");
+    if (n_launches < 1 || n_chunks < 0) return fail(h, FS_ERR_CONFIG, "n_launches must be >= 1, n_chunks >= 0");
     const fs_config &c = h->cfg;
     CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
+    if (n_chunks == 0) {
+        // automatic: as many chunks (up to 4) as still give every chunk half a wave of
+        // resident CTAs; small grids run as one chunk
+        int per_sm = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)h->k_metro, h->block, h->smem) !=
+            cudaSuccess)
+            cudaGetLastError();
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+        const long long half_wave = std::max(1ll, (long long)std::max(per_sm, 1) * std::max(sms, 1) / 2);
+        n_chunks = (int)std::max(1ll, std::min(4ll, (long long)h->grid / half_wave));
+    }
     if (h->d_snap) n_chunks = 1;
     n_chunks = std::min(n_chunks, std::min(h->grid, 64));
+    h->last_chunks = n_chunks;
     if (!h->s_in) CUDA_TRY(h, cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking), FS_ERR_CUDA);
     if (!h->s_out) CUDA_TRY(h, cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking), FS_ERR_CUDA);
     if (!h->s_comp2) CUDA_TRY(h, cudaStreamCreateWithFlags(&h->s_comp2, cudaStreamNonBlocking), FS_ERR_CUDA);
@@ -1095,6 +1113,13 @@ extern "C" int fs_run_host(fs_handle *h, const void *paths_in, void *paths_out, 
     CUDA_TRY(h, cudaStreamWaitEvent(h->stream, e_c2, 0), FS_ERR_CUDA);
     CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), FS_ERR_CUDA);
     h->timed = true;
+    return FS_OK;
+}
+
+extern "C" int fs_get_last_chunks(const fs_handle *h, int32_t *chunks)
+{
+    if (!h || !chunks) return FS_ERR_CONFIG;
+    *chunks = h->last_chunks;
     return FS_OK;
 }
 

@@ -162,17 +162,26 @@ extern "C" int fs_batch_create(int32_t n_types, const int32_t *type_dof, const c
     o << fsi_prelude(false) << "#define FS_NSKIP 0\n" << fsi_rng_src() << "\n";
     for (int k = 0; k < n_types; k++) {
         const int dof = b->type_dof[k];
+        // scalar-argument bodies; called rather than inlined for more than 8 DOF (see the
+        // same rule in fs_api.cu): the dispatcher holds every type's sweep
+        std::ostringstream args, call;
+        for (int d = 0; d < dof; d++) {
+            args << (d ? ", " : "") << "float x" << (d + 1);
+            call << (d ? ", " : "") << "x[" << d << "]";
+        }
+        const char *inl = dof > 8 ? "__device__ __noinline__ " : "__device__ __forceinline__ ";
         o << "namespace fs_type_" << k << " {\n" << fsi_float_literals(user_codes && user_codes[k] ? user_codes[k] : "")
-          << "\nstruct Sys {\n    static const int NOPS = " << n_ops << ";\n"
-          << "    static __device__ __forceinline__ float pot(const float *x) {\n";
-        for (int d = 0; d < dof; d++) o << "        const float x" << (d + 1) << " = x[" << d << "];\n";
-        o << "        return (" << fsi_float_literals(potentials[k]) << ");\n    }\n"
-          << "    static __device__ __forceinline__ void ops(const float *x, float *o) {\n";
-        for (int d = 0; d < dof; d++) o << "        const float x" << (d + 1) << " = x[" << d << "];\n";
+          << "\n" << inl << "float pot_s(" << args.str() << ") {\n        return ("
+          << fsi_float_literals(potentials[k]) << ");\n}\n"
+          << inl << "void ops_s(" << args.str() << ", float *o) {\n";
         for (int j = 0; j < n_ops; j++)
             o << "        o[" << j << "] = (" << fsi_float_literals(operators[k * n_ops + j]) << ");\n";
-        if (n_ops == 0) o << "        (void)x; (void)o;\n";
-        o << "    }\n};\n}\n";
+        if (n_ops == 0) o << "        (void)o;\n";
+        o << "}\nstruct Sys {\n    static const int NOPS = " << n_ops << ";\n"
+          << "    static __device__ __forceinline__ float pot(const float *x) { return pot_s(" << call.str()
+          << "); }\n"
+          << "    static __device__ __forceinline__ void ops(const float *x, float *o) { ops_s(" << call.str()
+          << ", o); }\n};\n}\n";
     }
     o << fsi_batch_src() << "\n";
     // one register budget for every CTA size up to 512, so the autotuner's candidates share

@@ -270,10 +270,10 @@ class PIMCKernel:
         if wait:
             self.sync()
 
-    def runHost(self, paths, out=None, launches=1, chunks=4):
+    def runHost(self, paths, out=None, launches=1, chunks=0):
         """setPaths(paths) + run(launches) + getPaths(out) as one pipelined call: the walkers
-        are split into ``chunks`` chunks whose host-to-device copy, sweeps and copy back
-        overlap (fs_run_host).  Same results bit for bit.  The copies overlap only when
+        are split into ``chunks`` chunks (0: automatic from the grid and the occupancy) whose
+        host-to-device copy, sweeps and copy back overlap (fs_run_host).  Same results bit for bit.  The copies overlap only when
         ``paths`` and ``out`` are page-locked (``pinHost``).  Returns ``out``."""
         a = np.asarray(paths)
         n = self._nbrOfWalkers * self._N * self._system.DOF
@@ -285,6 +285,9 @@ class PIMCKernel:
             raise ValueError("out must be a C-contiguous array of the paths' size and dtype")
         check(lib().fs_run_host(self._handle, a.ctypes.data, out.ctypes.data, int(launches), int(chunks)),
               self._handle)
+        used = ctypes.c_int32()
+        check(lib().fs_get_last_chunks(self._handle, ctypes.byref(used)), self._handle)
+        self.lastChunks = int(used.value)
         self._runsSinceZero += int(launches)
         self.sync()
         return out

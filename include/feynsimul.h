@@ -183,11 +183,14 @@ int fs_set_ranlux_tables(fs_handle *h, const uint32_t *tab, size_t n_tab_rows,
 int fs_run(fs_handle *h, int32_t n_launches);
 /* n_launches runs on host path buffers ([walkers][DOF][N] in the path precision; in and
  * out may be the same buffer), pipelined: the walkers are split into n_chunks chunks whose
- * copy-in, sweeps and copy-out overlap on three streams.  Equivalent to fs_set_paths +
+ * copy-in, sweeps and copy-out overlap on three streams (n_chunks = 0: automatic, up to 4
+ * chunks of at least half a wave of resident CTAs each).  Equivalent to fs_set_paths +
  * fs_run + fs_get_paths (kernel.py:567-574, :459-506, :557-565); asynchronous like fs_run
  * (the buffers must stay valid until fs_sync), and overlapping only for page-locked host
  * memory (fs_pin_host). */
 int fs_run_host(fs_handle *h, const void *paths_in, void *paths_out, int32_t n_launches, int32_t n_chunks);
+/* chunks the last fs_run_host call used (each chunk launches the sweep kernel n_launches times) */
+int fs_get_last_chunks(const fs_handle *h, int32_t *chunks);
 /* page-lock / release a host buffer (cudaHostRegister) for overlapped copies */
 int fs_pin_host(void *ptr, size_t bytes);
 int fs_unpin_host(void *ptr);
