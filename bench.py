@@ -546,7 +546,7 @@ def run_gb300(args, rank, world):
         "energy_mean": float(series[series.shape[0] // 2:].mean()),
         "energy_all_replicas": group.merge(series[series.shape[0] // 2:].mean(axis=0)),
         "acceptance_rate": float(k.getAcceptanceRate()),
-        "gpu_launches": args.steps * (1 + k.lastChunks),
+        "gpu_launches": args.steps * (2 + k.lastChunks),  # sweeps, pipelined chunks, walker reductions
         "roofline": roof, "clocks": clk,
     }
     k.close()
