@@ -111,3 +111,21 @@ def test_python_validation_matches_reference_messages():
 def test_float_literal_rewrite_in_generated_source():
     rc, log = _compile(_cfg(), "0.5 * x1 * x1 + 1e-3 + 2. * .25 + 0x1p-3")
     assert rc == 0, log
+
+
+def test_c_caller_links_and_compiles_a_sweep(tmp_path):
+    """tests/c/abi_check.c: the header and library used from C, as any FFI would."""
+    import shutil
+    import subprocess
+    L = _lib()
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    exe = str(tmp_path / "abi_check")
+    libdir = os.path.dirname(L.LIB_PATH)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "c", "abi_check.c"), "-L", libdir, "-lfeynsimul_gb300",
+                    "-Wl,-rpath," + libdir, "-o", exe], check=True)
+    env = dict(os.environ, FS_CACHE_DIR=str(tmp_path / "cache"))
+    r = subprocess.run([exe], capture_output=True, text=True, env=env, timeout=300)
+    assert r.returncode == 0 and "abi ok" in r.stdout, r.stdout + r.stderr
