@@ -1,10 +1,10 @@
 """Build recipe for ``oracle/_ref``: the reference's own OpenCL C compiled on the CPU.
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``tests/golden/make_golden.py`` and the
-oracle may use this module; the product never does.  It needs the reference tree, which
-exists only in the development container (``REFERENCE_ROOT``); everything it builds goes
-to ``oracle/_ref/`` (git-ignored).  The GPU machine never runs it: the goldens it produces
-are committed under ``tests/golden/``.
+oracle may use this module; the product never does.  It needs the reference's source tree
+(``REFERENCE_ROOT``); everything it builds goes to ``oracle/_ref/`` (git-ignored).  Where
+the tree is absent nothing here runs: the goldens it produces are committed under
+``tests/golden/``.
 
 What it does:
 

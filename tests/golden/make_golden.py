@@ -1,6 +1,6 @@
 """Generate the golden fixtures in tests/golden/ from the reference's own code.
 
-Run in the development container, where the reference tree exists:
+Run where the reference's source tree exists:
 
     python tests/golden/make_golden.py
 
