@@ -62,71 +62,78 @@ struct FsRanlux {
     fs_u32 dummy;   // padding word of the table, carried through unchanged
 };
 
-// cycle position p updates lag a = 23 - p from lag (a + 10) % 24
+// cycle position p updates lag a = 23 - p from lag (a + 10) % 24.  A chunk names only the
+// eight lag words it reads or writes (the 24-step cycle needs all of them).
 __device__ __forceinline__ void fs_rl_chunk4_p0(FsRanlux &r)
 {
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
-        "subc.cc.u32 %23, %9, %23;\n\t" "and.b32 %23, %23, -256;\n\t"
-        "subc.cc.u32 %22, %8, %22;\n\t" "and.b32 %22, %22, -256;\n\t"
-        "subc.cc.u32 %21, %7, %21;\n\t" "and.b32 %21, %21, -256;\n\t"
-        "subc.cc.u32 %20, %6, %20;\n\t" "and.b32 %20, %20, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
-        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %4;\n\t"
+        "subc.cc.u32 %0, %5, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
+        "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
+        "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
+        "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        : "+r"(r.s[23]), "+r"(r.s[22]), "+r"(r.s[21]), "+r"(r.s[20]), "+r"(r.carry)
+        : "r"(r.s[9]), "r"(r.s[8]), "r"(r.s[7]), "r"(r.s[6]));
 }
 
 __device__ __forceinline__ void fs_rl_chunk4_p4(FsRanlux &r)
 {
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
-        "subc.cc.u32 %19, %5, %19;\n\t" "and.b32 %19, %19, -256;\n\t"
-        "subc.cc.u32 %18, %4, %18;\n\t" "and.b32 %18, %18, -256;\n\t"
-        "subc.cc.u32 %17, %3, %17;\n\t" "and.b32 %17, %17, -256;\n\t"
-        "subc.cc.u32 %16, %2, %16;\n\t" "and.b32 %16, %16, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
-        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %4;\n\t"
+        "subc.cc.u32 %0, %5, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
+        "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
+        "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
+        "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        : "+r"(r.s[19]), "+r"(r.s[18]), "+r"(r.s[17]), "+r"(r.s[16]), "+r"(r.carry)
+        : "r"(r.s[5]), "r"(r.s[4]), "r"(r.s[3]), "r"(r.s[2]));
 }
 
 __device__ __forceinline__ void fs_rl_chunk4_p8(FsRanlux &r)
 {
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
-        "subc.cc.u32 %15, %1, %15;\n\t" "and.b32 %15, %15, -256;\n\t"
-        "subc.cc.u32 %14, %0, %14;\n\t" "and.b32 %14, %14, -256;\n\t"
-        "subc.cc.u32 %13, %23, %13;\n\t" "and.b32 %13, %13, -256;\n\t"
-        "subc.cc.u32 %12, %22, %12;\n\t" "and.b32 %12, %12, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
-        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %4;\n\t"
+        "subc.cc.u32 %0, %5, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
+        "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
+        "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
+        "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        : "+r"(r.s[15]), "+r"(r.s[14]), "+r"(r.s[13]), "+r"(r.s[12]), "+r"(r.carry)
+        : "r"(r.s[1]), "r"(r.s[0]), "r"(r.s[23]), "r"(r.s[22]));
 }
 
 __device__ __forceinline__ void fs_rl_chunk4_p12(FsRanlux &r)
 {
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
-        "subc.cc.u32 %11, %21, %11;\n\t" "and.b32 %11, %11, -256;\n\t"
-        "subc.cc.u32 %10, %20, %10;\n\t" "and.b32 %10, %10, -256;\n\t"
-        "subc.cc.u32 %9, %19, %9;\n\t" "and.b32 %9, %9, -256;\n\t"
-        "subc.cc.u32 %8, %18, %8;\n\t" "and.b32 %8, %8, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
-        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %4;\n\t"
+        "subc.cc.u32 %0, %5, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
+        "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
+        "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
+        "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        : "+r"(r.s[11]), "+r"(r.s[10]), "+r"(r.s[9]), "+r"(r.s[8]), "+r"(r.carry)
+        : "r"(r.s[21]), "r"(r.s[20]), "r"(r.s[19]), "r"(r.s[18]));
 }
 
 __device__ __forceinline__ void fs_rl_chunk4_p16(FsRanlux &r)
 {
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
-        "subc.cc.u32 %7, %17, %7;\n\t" "and.b32 %7, %7, -256;\n\t"
-        "subc.cc.u32 %6, %16, %6;\n\t" "and.b32 %6, %6, -256;\n\t"
-        "subc.cc.u32 %5, %15, %5;\n\t" "and.b32 %5, %5, -256;\n\t"
-        "subc.cc.u32 %4, %14, %4;\n\t" "and.b32 %4, %4, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
-        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %4;\n\t"
+        "subc.cc.u32 %0, %5, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
+        "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
+        "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
+        "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        : "+r"(r.s[7]), "+r"(r.s[6]), "+r"(r.s[5]), "+r"(r.s[4]), "+r"(r.carry)
+        : "r"(r.s[17]), "r"(r.s[16]), "r"(r.s[15]), "r"(r.s[14]));
 }
 
 __device__ __forceinline__ void fs_rl_chunk4_p20(FsRanlux &r)
 {
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %24;\n\t"
-        "subc.cc.u32 %3, %13, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "subc.cc.u32 %2, %12, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
-        "subc.cc.u32 %1, %11, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
-        "subc.cc.u32 %0, %10, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
-        : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
+    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %4;\n\t"
+        "subc.cc.u32 %0, %5, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
+        "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
+        "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
+        "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        : "+r"(r.s[3]), "+r"(r.s[2]), "+r"(r.s[1]), "+r"(r.s[0]), "+r"(r.carry)
+        : "r"(r.s[13]), "r"(r.s[12]), "r"(r.s[11]), "r"(r.s[10]));
 }
 
 __device__ __forceinline__ void fs_rl_cycle(FsRanlux &r)
