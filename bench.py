@@ -238,11 +238,19 @@ TUNED_WPB = {"he3": 4, "ho": 0}
 # The peak is the issue roof of the SMs: 4 schedulers x 32 lanes x 152 SMs per clock, at
 # the median SM clock sampled during the timed region (one lane op per lane per cycle).
 POT_OPS = {"he3": 138.0, "ho": 3.0}
+# lane operations per slice of one measurement: He3 the virial energy (3 pairs with the
+# LM2M2 derivative) and the 200-bin histogram of the 3 pair distances; HO x^2
+MEAS_OPS = {"he3": 3 * 60.0 + 3 * 12.0, "ho": 2.0}
 
 
 def alg_ops_per_node(config, ka):
+    """Algorithmic lane operations per node update: the move (random numbers, Box-Muller,
+    two potential evaluations) plus the launch's measurements spread over its node updates
+    (operators and histogram per slice, and for a correlator N/2 lags x N products, each a
+    multiply and an add)."""
     dof = 6 if config == "he3" else 1
     seg = 2 ** ka["S"]
+    N = ka["N"]
     uni = 2 * dof + 2.0 / (seg - 1)
     if ka["enableRanlux"]:
         nskip = {0: 0, 1: 24, 2: 76, 3: 200, 4: 380}[ka["luxuaryFactor"] + 1]
@@ -250,7 +258,13 @@ def alg_ops_per_node(config, ka):
     else:
         rng = uni * 8
     bm = dof * 9
-    return rng + bm + 2 * POT_OPS[config]
+    # one measurement per operator run, after metroStepsPerOperatorRun sweeps of
+    # (N / 2^S) * (2^S - 1) node updates per walker
+    nodes_between = ka["metroStepsPerOperatorRun"] * (N // seg) * (seg - 1)
+    meas = N * MEAS_OPS[config]
+    if ka.get("enableCorrelator"):
+        meas += len(ka.get("correlators") or ()) * (N // 2) * N * 2
+    return rng + bm + 2 * POT_OPS[config] + meas / nodes_between
 
 
 # DRAM bytes per fs_metropolis launch from one ncu capture of the default workload
