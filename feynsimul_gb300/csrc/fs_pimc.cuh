@@ -26,6 +26,7 @@
 #define FS_BLOCK (FS_WPB * FS_TPW)
 #define FS_LPT ((FS_HALF_N + FS_TPW - 1) / FS_TPW)  // correlator lags owned per thread
 #define FS_COR_REGS (FS_ACCUM != 3 && FS_LPT * FS_NCOR <= 16)
+#define FS_CSTEP (FS_N % 4 == 0 ? 4 : 1)  // FP64 correlator: partial sums over s1 mod 4
 
 // Shared-memory path layout.  Slice s of degree d of a walker sits at d * FS_DSTRIDE +
 // FS_PHYS(s) with one padding word after every 2^S slices: the segment threads of a walker
@@ -720,19 +721,52 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                             acc = FS_ADD(acc, FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]));
                         }
 #else
-#pragma unroll 4
-                    for (int s1 = 0; s1 < FS_N; s1++) {
 #if FS_ACCUM == 0
+#pragma unroll 4
+                    for (int s1 = 0; s1 < FS_N; s1++)
                         acc = FS_ADD(acc, FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]));
-#elif FS_ACCUM == 3
-                        const FT pr = FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]);
-                        acc.f = __fadd_rn(acc.f, (float)pr);
-                        fs_kahan(acc.ks, acc.kc, (float)pr);
-                        acc.d = __dadd_rn(acc.d, (double)pr);
 #else
-                        acc = __dadd_rn(acc, (double)FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]));
+                    // FP64 sums: four partial sums over s1 mod 4, combined at the end as
+                    // (p0 + p1) + (p2 + p3), p0 starting from the running sum.  Four
+                    // independent chains keep the FP64 pipe busy (a single chain of N
+                    // dependent adds made the lag loop latency bound).
+#if FS_ACCUM == 3
+                    double p0 = acc.d, p1 = 0.0, p2 = 0.0, p3 = 0.0;
+#else
+                    double p0 = acc, p1 = 0.0, p2 = 0.0, p3 = 0.0;
+#endif
+#pragma unroll 2
+                    for (int s1 = 0; s1 < FS_N; s1 += FS_CSTEP) {
+                        const FT q0 = FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]);
+                        p0 = __dadd_rn(p0, (double)q0);
+#if FS_CSTEP == 4
+                        const FT q1 = FS_MUL(Cc[s1 + 1], Cc[(s1 + 1 + tau) & (FS_N - 1)]);
+                        const FT q2 = FS_MUL(Cc[s1 + 2], Cc[(s1 + 2 + tau) & (FS_N - 1)]);
+                        const FT q3 = FS_MUL(Cc[s1 + 3], Cc[(s1 + 3 + tau) & (FS_N - 1)]);
+                        p1 = __dadd_rn(p1, (double)q1);
+                        p2 = __dadd_rn(p2, (double)q2);
+                        p3 = __dadd_rn(p3, (double)q3);
+#endif
+#if FS_ACCUM == 3
+                        // the study's FP32 columns: the same products in slice order
+                        acc.f = __fadd_rn(acc.f, (float)q0);
+                        fs_kahan(acc.ks, acc.kc, (float)q0);
+#if FS_CSTEP == 4
+                        acc.f = __fadd_rn(acc.f, (float)q1);
+                        fs_kahan(acc.ks, acc.kc, (float)q1);
+                        acc.f = __fadd_rn(acc.f, (float)q2);
+                        fs_kahan(acc.ks, acc.kc, (float)q2);
+                        acc.f = __fadd_rn(acc.f, (float)q3);
+                        fs_kahan(acc.ks, acc.kc, (float)q3);
+#endif
 #endif
                     }
+#if FS_ACCUM == 3
+                    acc.d = __dadd_rn(__dadd_rn(p0, p1), __dadd_rn(p2, p3));
+#else
+                    acc = __dadd_rn(__dadd_rn(p0, p1), __dadd_rn(p2, p3));
+#endif
+#endif
 #endif
 #if FS_COR_REGS
                     cacc[c][j] = acc;

@@ -172,12 +172,10 @@ template <int A>
 __device__ __forceinline__ float fs_rl_value(const FsRanlux &r)
 {
     const fs_u32 v = r.s[A];
-    float out = __fmul_rn(__uint2float_rn(v), 0x1p-32f);
-    if (v < (4096u << 8)) {  // value below 2^-12: add the next lag scaled by 2^-24
-        out = __fadd_rn(out, __fmul_rn(__uint2float_rn(r.s[(A + 9) % 24]), 0x1p-56f));
-        if (out == 0.0f) out = 0x1p-48f;
-    }
-    return out;
+    const float hi = __fmul_rn(__uint2float_rn(v), 0x1p-32f);
+    const float lo = __fmul_rn(__uint2float_rn(r.s[(A + 9) % 24]), 0x1p-56f);
+    float out = v < (4096u << 8) ? __fadd_rn(hi, lo) : hi;
+    return out == 0.0f ? 0x1p-48f : out;
 }
 
 // NSKIP steps starting at cycle position pos (a multiple of 4); returns the new position

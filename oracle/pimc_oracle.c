@@ -508,35 +508,47 @@ int fso_run(fso_args_t *A)
                             uint32_t s2 = (s1 + (uint32_t)tau) % FS_N;
                             corf[c][tau] = corf[c][tau] + fso_cor_prod(path, s1, s2, c);
                         }
-#elif FS_ACCUM == 3
-                    for (uint32_t s1 = 0; s1 < FS_N; s1++) {
-                        const FT pr = fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
-                        cor32[c][tau] = cor32[c][tau] + (float)pr;
-                        fso_kahan_add(&cork[c][tau], (float)pr);
-                        cord[c][tau] += (double)pr;
-                    }
 #else
-                    for (uint32_t s1 = 0; s1 < FS_N; s1++)
-                        cord[c][tau] += (double)fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
+                    {
+                        /* FP64 sums: partial sums over s1 mod 4, combined as (p0 + p1) + (p2 + p3)
+                         * (p0 from the running sum); the FP32 study columns in slice order */
+                        double p[4] = {cord[c][tau], 0.0, 0.0, 0.0};
+                        const uint32_t step = (FS_N % 4 == 0) ? 4u : 1u;
+                        for (uint32_t s1 = 0; s1 < FS_N; s1++) {
+                            const FT pr = fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
+                            p[s1 % step] += (double)pr;
+#if FS_ACCUM == 3
+                            cor32[c][tau] = cor32[c][tau] + (float)pr;
+                            fso_kahan_add(&cork[c][tau], (float)pr);
+#endif
+                        }
+                        cord[c][tau] = (p[0] + p[1]) + (p[2] + p[3]);
+                    }
 #endif
                 }
 #else
+#if FS_ACCUM == 0
             for (uint32_t s1 = 0; s1 < FS_N; s1++)
                 for (int tau = 0; tau < FS_HALF_N; tau++)
-                    for (int c = 0; c < FS_NCOR; c++) {
-#if FS_ACCUM == 0
+                    for (int c = 0; c < FS_NCOR; c++)
                         corf[c][tau] = corf[c][tau] + fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
-#elif FS_ACCUM == 3
-                    {
+#else
+            /* one lag at a time, the FP64 sums in the four-way order of the parallel mode */
+            for (int c = 0; c < FS_NCOR; c++)
+                for (int tau = 0; tau < FS_HALF_N; tau++) {
+                    double p[4] = {cord[c][tau], 0.0, 0.0, 0.0};
+                    const uint32_t step = (FS_N % 4 == 0) ? 4u : 1u;
+                    for (uint32_t s1 = 0; s1 < FS_N; s1++) {
                         const FT pr = fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
+                        p[s1 % step] += (double)pr;
+#if FS_ACCUM == 3
                         cor32[c][tau] = cor32[c][tau] + (float)pr;
                         fso_kahan_add(&cork[c][tau], (float)pr);
-                        cord[c][tau] += (double)pr;
-                    }
-#else
-                        cord[c][tau] += (double)fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
 #endif
                     }
+                    cord[c][tau] = (p[0] + p[1]) + (p[2] + p[3]);
+                }
+#endif
 #endif
 #endif
         }
