@@ -205,12 +205,21 @@ __device__ __forceinline__ fs_u32 fs_rl_skip(FsRanlux &r, fs_u32 pos)
     return (fs_u32)rem;
 }
 
-#define FS_RL_OUT4(P)                          \
-    fs_rl_chunk4_p##P(r);                      \
-    o0 = fs_rl_value<23 - P>(r);               \
-    o1 = fs_rl_value<22 - P>(r);               \
-    o2 = fs_rl_value<21 - P>(r);               \
-    o3 = fs_rl_value<20 - P>(r);
+// Four outputs: the plain conversion, and the small-value correction of fs_rl_value only
+// when some lane of the warp drew a value below 2^-12 (probability 2^-12 per value).
+#define FS_RL_OUT4(P)                                                                      \
+    fs_rl_chunk4_p##P(r);                                                                  \
+    o0 = __fmul_rn(__uint2float_rn(r.s[23 - P]), 0x1p-32f);                                \
+    o1 = __fmul_rn(__uint2float_rn(r.s[22 - P]), 0x1p-32f);                                \
+    o2 = __fmul_rn(__uint2float_rn(r.s[21 - P]), 0x1p-32f);                                \
+    o3 = __fmul_rn(__uint2float_rn(r.s[20 - P]), 0x1p-32f);                                \
+    if (__any_sync(__activemask(),                                                         \
+                   min(min(r.s[23 - P], r.s[22 - P]), min(r.s[21 - P], r.s[20 - P])) < (4096u << 8))) { \
+        o0 = fs_rl_value<23 - P>(r);                                                       \
+        o1 = fs_rl_value<22 - P>(r);                                                       \
+        o2 = fs_rl_value<21 - P>(r);                                                       \
+        o3 = fs_rl_value<20 - P>(r);                                                       \
+    }
 
 // four outputs (ranluxcl32), then the skip after every 24 outputs
 template <int NSKIP>
