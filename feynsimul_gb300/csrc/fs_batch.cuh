@@ -26,6 +26,7 @@ struct FsBatchSys {
     double *op_sums;         // [walkers][nops], accumulated over launches
     int n_walkers, N, S, tpw, wpb, nops, type, n_tiles;
     int op_runs, msteps;
+    int global;              // 1: the tile works on its walkers' rows of `paths` in place
     float eps;
     float sigma[FS_BATCH_MAX_S + 1];
 };
@@ -46,7 +47,10 @@ __device__ __forceinline__ void fs_walker_sync(int tpw, int wl)
 }
 
 // One tile: walkers [tile*wpb, ...) of system sd.  All threads of the CTA call it.
-template <int DOF, class Sys>
+// GLOBAL: the walkers' paths stay in device memory (L1/L2) and are worked on in place, for
+// walkers too large to put enough of them in shared memory to fill the CTA (the same
+// arithmetic as the shared-memory tile, like the sweep's global-path mode).
+template <int DOF, class Sys, bool GLOBAL>
 __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, float *smem, size_t old_slot_floats)
 {
     const int tid = threadIdx.x;
@@ -62,16 +66,18 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
     const int nthr = sd.wpb * tpw;
     // saved old segments: this CTA's slice of the global scratch, [(seg-1)*DOF][tile threads]
     float *s_old = sd.old_scratch + (size_t)blockIdx.x * old_slot_floats;
-    double *s_op = (double *)(smem + sd.wpb * wstride);  // [wpb][nops]
+    double *s_op = (double *)(GLOBAL ? smem : smem + sd.wpb * wstride);  // [wpb][nops]
 
-#define FSB_AT(P, d, s) (P)[(d) * dstride + (s) + ((s) >> S)]
+#define FSB_AT(P, d, s) (GLOBAL ? (P)[(d) * N + (s)] : (P)[(d) * dstride + (s) + ((s) >> S)])
     {
-        const size_t base = (size_t)w0 * DOF * N;
-        const int count = n_here * DOF * N;
-        for (int i = tid; i < count; i += blockDim.x) {
-            const int wi = i / (DOF * N), r = i - wi * (DOF * N);
-            const int d = r / N, sl = r - d * N;
-            FSB_AT(smem + wi * wstride, d, sl) = sd.paths[base + i];
+        if (!GLOBAL) {
+            const size_t base = (size_t)w0 * DOF * N;
+            const int count = n_here * DOF * N;
+            for (int i = tid; i < count; i += blockDim.x) {
+                const int wi = i / (DOF * N), r = i - wi * (DOF * N);
+                const int d = r / N, sl = r - d * N;
+                FSB_AT(smem + wi * wstride, d, sl) = sd.paths[base + i];
+            }
         }
         for (int i = tid; i < sd.wpb * sd.nops; i += blockDim.x) s_op[i] = 0.0;
     }
@@ -79,7 +85,7 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
 
     if (active) {
         const int w = w0 + wl;
-        float *P = smem + wl * wstride;
+        float *P = GLOBAL ? sd.paths + (size_t)w * DOF * N : smem + wl * wstride;
         const int th = w * tpw + t;
         FsXorshift g, ws;
         {
@@ -173,12 +179,14 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
     }
     __syncthreads();
     {
-        const size_t base = (size_t)w0 * DOF * N;
-        const int count = n_here * DOF * N;
-        for (int i = tid; i < count; i += blockDim.x) {
-            const int wi = i / (DOF * N), r = i - wi * (DOF * N);
-            const int d = r / N, sl = r - d * N;
-            sd.paths[base + i] = FSB_AT(smem + wi * wstride, d, sl);
+        if (!GLOBAL) {
+            const size_t base = (size_t)w0 * DOF * N;
+            const int count = n_here * DOF * N;
+            for (int i = tid; i < count; i += blockDim.x) {
+                const int wi = i / (DOF * N), r = i - wi * (DOF * N);
+                const int d = r / N, sl = r - d * N;
+                sd.paths[base + i] = FSB_AT(smem + wi * wstride, d, sl);
+            }
         }
         for (int i = tid; i < n_here * sd.nops; i += blockDim.x) sd.op_sums[(size_t)w0 * sd.nops + i] += s_op[i];
     }

@@ -32,6 +32,7 @@ struct FsBatchSysHost {  // mirrors FsBatchSys in fs_batch.cuh
     double *op_sums;
     int n_walkers, N, S, tpw, wpb, nops, type, n_tiles;
     int op_runs, msteps;
+    int global;
     float eps;
     float sigma[FS_BATCH_MAX_S + 1];
 };
@@ -39,6 +40,7 @@ struct FsBatchSysHost {  // mirrors FsBatchSys in fs_batch.cuh
 struct fs_batch {
     int device = 0;
     std::vector<fs_batch_system> sys;
+    std::vector<int> sys_global;  // per system: paths worked on in device memory
     std::vector<int> type_dof;
     std::vector<FsBatchSysHost> desc;
     int n_ops = 0, block = 256, grid = 0;
@@ -140,16 +142,27 @@ extern "C" int fs_batch_create(int32_t n_types, const int32_t *type_dof, const c
             free_batch(b);
             return bfail(FS_ERR_CONFIG, "system %d: N / 2^S = %d threads per walker does not fit the block", i, tpw);
         }
-        int wpb = s.walkers_per_tile > 0 ? s.walkers_per_tile : block_threads / tpw;
-        wpb = std::min(wpb, block_threads / tpw);
-        if (tpw > 32) wpb = std::min(wpb, 15);  // named barriers 1..15
+        int wpb_max = std::min(s.walkers_per_tile > 0 ? s.walkers_per_tile : block_threads, block_threads / tpw);
+        if (tpw > 32) wpb_max = std::min(wpb_max, 15);  // named barriers 1..15
+        int wpb = wpb_max;
         while (wpb > 1 && tile_smem_bytes(dof, s.n_slices, s.bisection_level, wpb, n_ops) > 200 * 1024) wpb--;
-        if (tile_smem_bytes(dof, s.n_slices, s.bisection_level, wpb, n_ops) > 220 * 1024) {
-            free_batch(b);
-            return bfail(FS_ERR_CONFIG, "system %d: one walker's path does not fit in shared memory", i);
+        // walkers so large that shared memory holds too few of them to fill half the CTA
+        // (large clusters at N = 1024) work on their paths in device memory instead
+        const bool global = wpb * tpw * 2 < block_threads && dof > 8;
+        size_t tile_bytes;
+        if (global) {
+            wpb = wpb_max;
+            tile_bytes = (size_t)wpb * std::max(n_ops, 1) * 8;
+        } else {
+            tile_bytes = tile_smem_bytes(dof, s.n_slices, s.bisection_level, wpb, n_ops);
+            if (tile_bytes > 220 * 1024) {
+                free_batch(b);
+                return bfail(FS_ERR_CONFIG, "system %d: one walker's path does not fit in shared memory", i);
+            }
         }
+        b->sys_global.push_back(global ? 1 : 0);
         s.walkers_per_tile = wpb;
-        max_smem = std::max(max_smem, tile_smem_bytes(dof, s.n_slices, s.bisection_level, wpb, n_ops));
+        max_smem = std::max(max_smem, tile_bytes);
         const size_t seg = (size_t)1 << s.bisection_level;
         max_old = std::max(max_old, (seg - 1) * dof * (size_t)(wpb * tpw));
         b->node_updates += (long long)s.n_walkers * tpw * (long long)(seg - 1) * op_runs * msteps;
@@ -199,10 +212,15 @@ extern "C" int fs_batch_create(int32_t n_types, const int32_t *type_dof, const c
          "        if (it >= n_items) break;\n"
          "        const FsBatchItem item = items[it];\n"
          "        const FsBatchSys &sd = sys[item.sys];\n"
-         "        switch (sd.type) {\n";
+         "        switch (sd.type * 2 + sd.global) {\n";
+    // one case per (type, path placement) pair the batch uses
+    std::vector<char> used(2 * n_types, 0);
+    for (int i = 0; i < n_systems; i++) used[2 * b->sys[i].type + b->sys_global[i]] = 1;
     for (int k = 0; k < n_types; k++)
-        o << "        case " << k << ": fs_batch_tile<" << b->type_dof[k] << ", fs_type_" << k
-          << "::Sys>(sd, item.tile, fsb_smem, old_slot); break;\n";
+        for (int g = 0; g < 2; g++)
+            if (used[2 * k + g])
+                o << "        case " << (2 * k + g) << ": fs_batch_tile<" << b->type_dof[k] << ", fs_type_" << k
+                  << "::Sys, " << (g ? "true" : "false") << ">(sd, item.tile, fsb_smem, old_slot); break;\n";
     o << "        default: break;\n        }\n    }\n}\n";
     b->source = o.str();
     std::string cubin;
@@ -264,6 +282,7 @@ extern "C" int fs_batch_create(int32_t n_types, const int32_t *type_dof, const c
         d.n_tiles = (s.n_walkers + d.wpb - 1) / d.wpb;
         d.op_runs = op_runs;
         d.msteps = msteps;
+        d.global = b->sys_global[i];
         // epsilon and the bisection widths in FP32 as the single-system kernel forms them
         char lit[64];
         snprintf(lit, sizeof lit, "%1.17e", s.beta / (double)s.n_slices);
