@@ -160,16 +160,20 @@ def cpu_cores():
 
 def oracle_cpu_rate(sysm, ka, extra, seconds=10.0, walkers=None):
     """Node updates/s of the oracle's C restatement (the reference algorithm) on the host
-    cores, on a bounded sample: a subset of walkers and fewer sweeps, sized to ~seconds."""
+    cores, on a bounded sample: a subset of walkers and fewer operator runs, sized to
+    ~seconds, with the workload's measurement cadence (metroStepsPerOperatorRun sweeps per
+    measurement of the operators, correlators and histograms)."""
     from oracle import oracle as orc
     cores = cpu_cores()
     W = walkers or max(cores * 4, 64)
     W = min(W, ka["nbrOfWalkers"])
 
-    def make(sweeps):
+    msteps = int(ka["metroStepsPerOperatorRun"])
+
+    def make(runs):
         cfg = orc.OracleConfig(
             DOF=sysm.DOF, potential=sysm.potential, userCode=sysm.userCode, nbrOfWalkers=W, N=ka["N"],
-            beta=ka["beta"], S=ka["S"], operatorRuns=1, metroStepsPerOperatorRun=sweeps,
+            beta=ka["beta"], S=ka["S"], operatorRuns=runs, metroStepsPerOperatorRun=msteps,
             nbrOfWalkersPerWorkGroup=1, enableParallelizePath=True, enableRanlux=ka["enableRanlux"],
             luxuaryFactor=ka.get("luxuaryFactor", 2), ranluxIntMax=ka.get("ranluxIntMax", 2 ** 32 - 1),
             operators=ka["operators"], correlators=ka.get("correlators", ()) or (), compat=False, accum=1,
@@ -186,20 +190,27 @@ def oracle_cpu_rate(sysm, ka, extra, seconds=10.0, walkers=None):
             o.walker_seeds[...] = rs.randint(0, 2 ** 31 - 1, size=o.walker_seeds.shape)
         return o, cfg
 
-    o, cfg = make(1)
-    t0 = time.perf_counter()
-    o.run()
-    t1 = time.perf_counter() - t0
-    sweeps = int(max(1, min(2000, seconds / max(t1, 1e-4))))
-    o, cfg = make(sweeps)
+    # calibrate on growing samples until one takes a tenth of the target, then scale
+    runs = 4
+    while True:
+        o, cfg = make(runs)
+        t0 = time.perf_counter()
+        o.run()
+        t1 = time.perf_counter() - t0
+        if t1 >= 0.1 * seconds or runs >= 10 ** 6:
+            break
+        runs = int(min(10 ** 6, runs * max(2.0, 0.15 * seconds / max(t1, 1e-6))))
+    runs = int(max(1, min(10 ** 6, runs * seconds / max(t1, 1e-6))))
+    o, cfg = make(runs)
     t0 = time.perf_counter()
     o.run()
     dt = time.perf_counter() - t0
     seg = 2 ** ka["S"]
+    sweeps = runs * msteps
     nodes = W * (ka["N"] // seg) * (seg - 1) * sweeps
     return {"value": nodes / dt, "unit": "node-updates/s", "cores": cores, "kind": "port",
-            "sample": f"{W} walkers x {sweeps} sweeps of the same system ({nodes} node updates, {dt:.1f} s), "
-                      f"oracle C restatement, OpenMP over walkers"}
+            "sample": f"{W} walkers x {sweeps} sweeps of the same system, one measurement every {msteps} "
+                      f"sweep(s) ({nodes} node updates, {dt:.1f} s), oracle C restatement, OpenMP over walkers"}
 
 
 def integrated_autocorr(series):
@@ -269,7 +280,7 @@ def alg_ops_per_node(config, ka):
 
 # DRAM bytes per fs_metropolis launch from one ncu capture of the default workload
 # (dram__bytes_read.sum + dram__bytes_write.sum; profiles/fs_metropolis_he3_lm2m2_ranlux.md)
-TRAFFIC_PER_LAUNCH = {"he3": 226.3e6}
+TRAFFIC_PER_LAUNCH = {"he3": 227.7e6}
 
 
 def roofline_for(config, ka, node_rate, clk, default_workload=True):

@@ -66,6 +66,8 @@ struct fs_handle {
     std::vector<std::string> ops, cors, hists;
     // launch geometry
     int tpw = 1, seg = 1, wpb = 1, block = 1, grid = 1;
+    int cor_ilv = 0;  // correlator lags summed in one slice pass over a doubled slice buffer
+    long long cwstride = 0;  // per-walker correlator buffer in shared memory, elements
     long long wstride = 0, vstride = 0;
     long long n_threads = 0;
     size_t smem = 0;
@@ -316,7 +318,8 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << lit(c.beta / (double)c.n_slices) << "\n#define FS_OPNORM " << lit(opnorm)
       << "\n#define FS_BINS " << (c.enable_bins ? 1 : 0) << "\n#define FS_NHIST " << nhist
       << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n#define FS_GLOBAL " << (c.global_path ? 1 : 0)
-      << "\n#define FS_VCACHE " << (h.vstride ? 1 : 0) << "\n#define FS_VSTRIDE " << h.vstride << "\n";
+      << "\n#define FS_VCACHE " << (h.vstride ? 1 : 0) << "\n#define FS_VSTRIDE " << h.vstride
+      << "\n#define FS_COR_ILV " << h.cor_ilv << "\n#define FS_CWSTRIDE " << h.cwstride << "\n";
     {
         const int mv = c.moves ? c.moves : FS_MOVE_BISECTION;
         const double nb = (double)c.n_slices / c.beta;
@@ -503,6 +506,21 @@ static int load_module(fs_handle *h, const std::string &cubin)
 // ------------------------------------------------------------------ validation
 // The checks of kernel.py:93-211 that concern the device path; the Python layer raises the
 // reference's exception types before it gets here.
+// SMs of the current device (152 on a GB300, also the answer without a device, for
+// compile-only use)
+static int device_sms()
+{
+    static const int sms = [] {
+        int dev = 0, n = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0)
+            return n;
+        (void)cudaGetLastError();
+        return 152;
+    }();
+    return sms;
+}
+
 static int validate(const fs_config &c, int nops, int ncor, int nhist)
 {
     if (c.dof < 1 || c.dof > 256) return fail(nullptr, FS_ERR_CONFIG, "DOF must be in [1, 256]");
@@ -607,6 +625,22 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     h->tpw = c.enable_parallelize_path ? (c.n_slices >> c.bisection_level) : 1;
     h->n_threads = (long long)c.n_walkers * h->tpw;
     h->ft = c.enable_double ? 8 : 4;
+    {
+        // float-float correlator sums (FP64 / Kahan modes, FP32 builds) with at most 4 lags per
+        // thread run every lag in one pass over the slice values, stored twice in a row so
+        // that slice s1 + tau needs no wrap
+        const long long lpt = (c.n_slices / 2 + h->tpw - 1) / h->tpw;
+        h->cor_ilv = ((c.accum == 1 || c.accum == 2) && !c.enable_double && lpt <= 4) ? 1 : 0;
+        // per-walker stride an odd multiple of 64 bytes: two walkers sharing a warp read
+        // opposite bank halves
+        const long long q = 64 / (long long)h->ft;
+        long long cw = (long long)h->cors.size() * c.n_slices * (h->cor_ilv ? 2 : 1);
+        if (cw) {
+            cw = ((cw + q - 1) / q) * q;
+            if ((cw / q) % 2 == 0) cw += q;
+        }
+        h->cwstride = cw;
+    }
     // padded shared-memory path (see FS_PHYS in fs_pimc.cuh): one word after every 2^S
     // slices; the walker stride is an odd multiple of 16 words
     const long long dstride = c.n_slices + (c.n_slices >> c.bisection_level);
@@ -620,7 +654,7 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     long long vstride = ((dstride + 15) / 16) * 16;
     if ((vstride / 16) % 2 == 0) vstride += 16;
     const size_t per_walker_base =
-        (size_t)((c.global_path ? 0 : wstride) + (long long)h->cors.size() * c.n_slices) * h->ft;
+        (size_t)((c.global_path ? 0 : wstride) + h->cwstride) * h->ft;
     // the path-shift and single-node moves change slices outside the bisection's
     // bookkeeping, so they go without the potential cache
     const bool other_moves = (c.moves & (FS_MOVE_PATH_SHIFT | FS_MOVE_SINGLE_NODE)) != 0;
@@ -676,13 +710,16 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
         h->smem = per_walker * h->wpb + hist_bytes;
     }
     // Register budget: unless the caller fixes it, compile for as many CTAs per SM as shared
-    // memory admits (<= 2048 threads per SM, >= 64 registers per thread).  Without the bound
-    // the compiler spends registers freely and the large kernels drop to one CTA per SM.
+    // memory admits (<= 2048 threads per SM, >= 64 registers per thread) and as the grid can
+    // put on one SM.  Without the bound the compiler spends registers freely and the large
+    // kernels drop to one CTA per SM; a grid of at most one CTA per SM gets every register.
     if (h->cfg.min_blocks_per_sm == 0) {
         long long by_smem = (227ll * 1024) / std::max<long long>(1, (long long)h->smem + 1024);
         long long by_threads = 2048 / h->block;
         long long by_regs = 65536 / (64ll * h->block);
-        h->cfg.min_blocks_per_sm = (int)std::max(1ll, std::min(std::min(by_smem, by_threads), by_regs));
+        long long by_grid = (h->grid + device_sms() - 1) / device_sms();
+        h->cfg.min_blocks_per_sm =
+            (int)std::max(1ll, std::min(std::min(std::min(by_smem, by_threads), by_regs), by_grid));
     }
     if (h->smem > 227 * 1024) {
         delete h;

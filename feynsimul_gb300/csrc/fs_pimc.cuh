@@ -27,6 +27,25 @@
 #define FS_LPT ((FS_HALF_N + FS_TPW - 1) / FS_TPW)  // correlator lags owned per thread
 #define FS_COR_REGS (FS_ACCUM != 3 && FS_LPT * FS_NCOR <= 16)
 #define FS_CSTEP (FS_N % 4 == 0 ? 4 : 1)  // FP64 correlator: partial sums over s1 mod 4
+// Correlator sums of the FP64 and Kahan modes in FP32 builds: float-float per measurement
+// (fs_ff_add), then one FP64 add per lag.  FS_COR_ILV (set by the host, which sizes shared
+// memory for it): a thread owning at most 4 lags sums them in one pass over the slice values,
+// which are stored twice in a row (FS_CSTRIDE = 2N words per correlator) so that slice
+// s1 + tau is read without a wrap.
+#define FS_COR_FF ((FS_ACCUM == 1 || FS_ACCUM == 2) && !FS_DOUBLE)
+#ifndef FS_COR_ILV
+#define FS_COR_ILV 0
+#endif
+#if FS_COR_ILV && !(FS_COR_FF && FS_LPT <= 4 && FS_LPT * FS_TPW <= FS_N)
+#error "FS_COR_ILV needs float-float correlator sums and at most 4 lags per thread"
+#endif
+#define FS_CSTRIDE (FS_COR_ILV ? 2 * FS_N : FS_N)
+#ifndef FS_CWSTRIDE
+#define FS_CWSTRIDE (FS_NCOR * FS_CSTRIDE)  // per-walker correlator buffer (the host pads it)
+#endif
+#if FS_CWSTRIDE < FS_NCOR * FS_CSTRIDE
+#error "per-walker correlator buffer smaller than its slice values"
+#endif
 
 // Shared-memory path layout.  Slice s of degree d of a walker sits at d * FS_DSTRIDE +
 // FS_PHYS(s) with one padding word after every 2^S slices: the segment threads of a walker
@@ -408,6 +427,41 @@ struct FsCorAcc {
 typedef double FsCorAcc;
 #endif
 
+// FP32 -> FP64 on the integer pipe (GB300's FP64 pipe is narrow, and the FP64 sums spend
+// one conversion per term there): exact for every value a flush-to-zero build produces --
+// normal numbers and signed zeros; infinities and NaNs kept.  The sign moves to bit 63, the
+// exponent is rebiased by 1023 - 127, the mantissa moves up by 29 bits.  IEEE builds (which
+// can produce denormals) convert in hardware.
+__device__ __forceinline__ double fs_f2d(float x)
+{
+#if FS_FAST && !FS_DOUBLE
+    const unsigned u = __float_as_uint(x);
+    const unsigned e = (u >> 23) & 0xFFu;
+    const unsigned sign = u & 0x80000000u;
+    unsigned hi;
+    if (e == 0u) hi = sign;
+    else if (e == 0xFFu) hi = sign | 0x7FF00000u | ((u & 0x7FFFFFu) >> 3);
+    else hi = sign | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+#else
+    return (double)x;
+#endif
+}
+__device__ __forceinline__ double fs_f2d(double x) { return x; }
+
+// float-float accumulation: Knuth's TwoSum yields the exact rounding error of s + q, and the
+// errors are summed on the side (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM
+// J. Sci. Comput. 26 (2005), Algorithm 4.4 "Sum2"); s + e then carries about 48 significant
+// bits.  Explicitly rounded adds, so no contraction or reassociation can touch the steps.
+__device__ __forceinline__ void fs_ff_add(float &s, float &e, float q)
+{
+    const float t = __fadd_rn(s, q);
+    const float bp = __fsub_rn(t, s);
+    const float ap = __fsub_rn(t, bp);
+    e = __fadd_rn(e, __fadd_rn(__fsub_rn(s, ap), __fsub_rn(q, bp)));
+    s = t;
+}
+
 __device__ __forceinline__ void fs_kahan(float &s, float &c, float x)
 {
     const float y = __fsub_rn(x, c);
@@ -435,8 +489,8 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     FT *s_path = (FT *)fs_smem;                                  // [WPB][DOF*N]
     FT *s_v = s_path + FS_WPB * FS_WSTRIDE;                      // [WPB][VSTRIDE] (FS_VCACHE)
 #endif
-    FT *s_cor = s_v + FS_WPB * FS_VSTRIDE;                       // [WPB][NCOR][N]
-    fs_u32 *s_hist = (fs_u32 *)(s_cor + FS_WPB * FS_NCOR * FS_N);  // [HBINS]
+    FT *s_cor = s_v + FS_WPB * FS_VSTRIDE;                     // [WPB][CWSTRIDE >= NCOR * CSTRIDE]
+    fs_u32 *s_hist = (fs_u32 *)(s_cor + FS_WPB * FS_CWSTRIDE);  // [HBINS]
 
     const int tid_b = threadIdx.x;
     const int wl = tid_b / FS_TPW;
@@ -530,7 +584,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #endif
 #if FS_NCOR > 0
         FsCorAcc *g_cor = (FsCorAcc *)a.cor_means + (size_t)w * FS_NCOR * FS_HALF_N;
-        FT *C = s_cor + wl * FS_NCOR * FS_N;
+        FT *C = s_cor + wl * FS_CWSTRIDE;
 #if FS_COR_REGS
         FsCorAcc cacc[FS_NCOR][FS_LPT];
 #pragma unroll
@@ -644,13 +698,13 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #if FS_ACCUM == 0
                     opr[i] = FS_ADD(opr[i], ov[i]);
 #elif FS_ACCUM == 1
-                    opd[i] = __dadd_rn(opd[i], (double)ov[i]);
+                    opd[i] = __dadd_rn(opd[i], fs_f2d(ov[i]));
 #elif FS_ACCUM == 2
                     fs_kahan(opks[i], opkc[i], (float)ov[i]);
 #else
                     opf[i] = __fadd_rn(opf[i], (float)ov[i]);
                     fs_kahan(opks[i], opkc[i], (float)ov[i]);
-                    opd[i] = __dadd_rn(opd[i], (double)ov[i]);
+                    opd[i] = __dadd_rn(opd[i], fs_f2d(ov[i]));
 #endif
                 }
 #endif
@@ -686,7 +740,12 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                     FT cv[FS_NCOR];
                     fs_cors(FS_ARGS_AT(P, s), cv);
 #pragma unroll
-                    for (int c = 0; c < FS_NCOR; c++) C[c * FS_N + s] = cv[c];
+                    for (int c = 0; c < FS_NCOR; c++) {
+                        C[c * FS_CSTRIDE + s] = cv[c];
+#if FS_COR_ILV
+                        C[c * FS_CSTRIDE + s + FS_N] = cv[c];
+#endif
+                    }
                 }
 #endif
             }
@@ -695,7 +754,37 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             // lags tau = t + j*TPW owned by this thread
 #pragma unroll
             for (int c = 0; c < FS_NCOR; c++) {
-                const FT *Cc = C + c * FS_N;
+                const FT *Cc = C + c * FS_CSTRIDE;
+#if FS_COR_ILV
+                // every lag this thread owns in one pass over the slices: 2 x FS_LPT independent
+                // float-float chains, and Cc[s1] loaded once for all lags.  Unrolled by 8 (HO,
+                // N=128, 4 lags: 0.78 / 0.61 / 0.53 / 0.47 ms per launch for 1 / 2 / 4 / 8;
+                // a full unroll, 0.81 ms, misses the instruction cache).  Lags past N/2 (when
+                // FS_TPW does not divide N/2) are summed and dropped; s1 + tau < N + LPT * TPW
+                // <= 2N stays inside the doubled slice values.
+                {
+                    float fs[FS_LPT], fe[FS_LPT];
+#pragma unroll
+                    for (int j = 0; j < FS_LPT; j++) { fs[j] = 0.0f; fe[j] = 0.0f; }
+#pragma unroll 8
+                    for (int s1 = 0; s1 < FS_N; s1++) {
+                        const FT c0 = Cc[s1];
+#pragma unroll
+                        for (int j = 0; j < FS_LPT; j++)
+                            fs_ff_add(fs[j], fe[j], FS_MUL(c0, Cc[s1 + t + j * FS_TPW]));
+                    }
+#pragma unroll
+                    for (int j = 0; j < FS_LPT; j++) {
+                        const double m = __dadd_rn(fs_f2d(fs[j]), fs_f2d(fe[j]));
+#if FS_COR_REGS
+                        cacc[c][j] = __dadd_rn(cacc[c][j], m);
+#else
+                        const int tau = t + j * FS_TPW;
+                        if (tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = __dadd_rn(g_cor[c * FS_HALF_N + tau], m);
+#endif
+                    }
+                }
+#else
 #if FS_COR_REGS
 #pragma unroll
 #else
@@ -709,7 +798,15 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #else
                     FsCorAcc acc = g_cor[c * FS_HALF_N + tau];
 #endif
-#if FS_ACCUM == 0 && FS_PARALLEL
+#if FS_COR_FF
+                    {
+                        float fs = 0.0f, fe = 0.0f;
+#pragma unroll 4
+                        for (int s1 = 0; s1 < FS_N; s1++)
+                            fs_ff_add(fs, fe, FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]));
+                        acc = __dadd_rn(acc, __dadd_rn(fs_f2d(fs), fs_f2d(fe)));
+                    }
+#elif FS_ACCUM == 0 && FS_PARALLEL
                     // the reference's summation order (kernel.c:736-793)
 #pragma unroll 1
                     for (int k = 0; k < FS_SEG; k++)
@@ -738,14 +835,14 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #pragma unroll 2
                     for (int s1 = 0; s1 < FS_N; s1 += FS_CSTEP) {
                         const FT q0 = FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]);
-                        p0 = __dadd_rn(p0, (double)q0);
+                        p0 = __dadd_rn(p0, fs_f2d(q0));
 #if FS_CSTEP == 4
                         const FT q1 = FS_MUL(Cc[s1 + 1], Cc[(s1 + 1 + tau) & (FS_N - 1)]);
                         const FT q2 = FS_MUL(Cc[s1 + 2], Cc[(s1 + 2 + tau) & (FS_N - 1)]);
                         const FT q3 = FS_MUL(Cc[s1 + 3], Cc[(s1 + 3 + tau) & (FS_N - 1)]);
-                        p1 = __dadd_rn(p1, (double)q1);
-                        p2 = __dadd_rn(p2, (double)q2);
-                        p3 = __dadd_rn(p3, (double)q3);
+                        p1 = __dadd_rn(p1, fs_f2d(q1));
+                        p2 = __dadd_rn(p2, fs_f2d(q2));
+                        p3 = __dadd_rn(p3, fs_f2d(q3));
 #endif
 #if FS_ACCUM == 3
                         // the study's FP32 columns: the same products in slice order
@@ -774,6 +871,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                     g_cor[c * FS_HALF_N + tau] = acc;
 #endif
                 }
+#endif
             }
 #endif
             FS_WSYNC();

@@ -264,6 +264,22 @@ static inline void fso_kahan_add(fso_kahan_t *k, float x)
     k->s = t;
 }
 
+/* Correlator sums of the FP64 and Kahan modes in FP32 builds: one measurement's N products of
+ * a lag are summed in float-float -- Knuth's TwoSum gives the rounding error of every add
+ * exactly, and the errors are summed on the side (Ogita, Rump and Oishi, "Accurate sum and
+ * dot product", SIAM J. Sci. Comput. 26 (2005), Algorithm 4.4 "Sum2") -- and s + e joins the
+ * lag's FP64 running sum.  The error of the measurement's sum is bounded by about
+ * N * 2^-48 * sum |products|, far below the FP32 rounding of the products themselves. */
+#define FSO_COR_FF ((FS_ACCUM == 1 || FS_ACCUM == 2) && !FS_DOUBLE)
+static inline void fso_ff_add(float *s, float *e, float q)
+{
+    const float t = *s + q;
+    const float bp = t - *s;
+    const float ap = t - bp;
+    *e = *e + ((*s - ap) + (q - bp));
+    *s = t;
+}
+
 /* precision-study correlator accumulator (FS_ACCUM 3): the same products summed in
  * plain FP32, Kahan-compensated FP32 and FP64; 24 bytes, the device's layout */
 typedef struct {
@@ -508,6 +524,13 @@ int fso_run(fso_args_t *A)
                             uint32_t s2 = (s1 + (uint32_t)tau) % FS_N;
                             corf[c][tau] = corf[c][tau] + fso_cor_prod(path, s1, s2, c);
                         }
+#elif FSO_COR_FF
+                    {
+                        float fs = 0.0f, fe = 0.0f;
+                        for (uint32_t s1 = 0; s1 < FS_N; s1++)
+                            fso_ff_add(&fs, &fe, fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c));
+                        cord[c][tau] = cord[c][tau] + ((double)fs + (double)fe);
+                    }
 #else
                     {
                         /* FP64 sums: partial sums over s1 mod 4, combined as (p0 + p1) + (p2 + p3)
@@ -532,6 +555,15 @@ int fso_run(fso_args_t *A)
                 for (int tau = 0; tau < FS_HALF_N; tau++)
                     for (int c = 0; c < FS_NCOR; c++)
                         corf[c][tau] = corf[c][tau] + fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
+#elif FSO_COR_FF
+            /* one lag at a time, float-float as in the parallel mode */
+            for (int c = 0; c < FS_NCOR; c++)
+                for (int tau = 0; tau < FS_HALF_N; tau++) {
+                    float fs = 0.0f, fe = 0.0f;
+                    for (uint32_t s1 = 0; s1 < FS_N; s1++)
+                        fso_ff_add(&fs, &fe, fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c));
+                    cord[c][tau] = cord[c][tau] + ((double)fs + (double)fe);
+                }
 #else
             /* one lag at a time, the FP64 sums in the four-way order of the parallel mode */
             for (int c = 0; c < FS_NCOR; c++)
