@@ -542,7 +542,7 @@ def run_gb300(args, rank, world):
             pass
     e2e_value = nodes * args.steps * world / t_e2e
     h2d = host_paths.nbytes
-    d2h = k._nbrOfThreads * len(ka["operators"]) * 8 + host_paths.nbytes
+    d2h = ops.nbytes + host_paths.nbytes   # per-walker operator means + the paths
 
     # energy ESS/s from the per-run per-walker energy series of the e2e loop
     series = np.array(energies)  # [steps, walkers]

@@ -68,6 +68,7 @@ struct fs_handle {
     int tpw = 1, seg = 1, wpb = 1, block = 1, grid = 1;
     int cor_ilv = 0;  // correlator lags summed in one slice pass over a doubled slice buffer
     long long cwstride = 0;  // per-walker correlator buffer in shared memory, elements
+    int resident_per_sm = 0;  // resident CTAs per SM of the sweep kernel (fs_run_host), 0 = not yet queried
     long long wstride = 0, vstride = 0;
     long long n_threads = 0;
     size_t smem = 0;
@@ -1082,17 +1083,44 @@ extern "C" int fs_run_host(fs_handle *h, const void *paths_in, void *paths_out, 
     if (n_chunks == 0) {
         // automatic: as many chunks (up to 4) as still give every chunk half a wave of
         // resident CTAs; small grids run as one chunk
-        int per_sm = 0, sms = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)h->k_metro, h->block, h->smem) !=
-            cudaSuccess)
-            cudaGetLastError();
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-        const long long half_wave = std::max(1ll, (long long)std::max(per_sm, 1) * std::max(sms, 1) / 2);
+        if (!h->resident_per_sm) {
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)h->k_metro, h->block, h->smem) !=
+                cudaSuccess)
+                cudaGetLastError();
+            h->resident_per_sm = std::max(per_sm, 1);
+        }
+        const long long half_wave = std::max(1ll, (long long)h->resident_per_sm * device_sms() / 2);
         n_chunks = (int)std::max(1ll, std::min(4ll, (long long)h->grid / half_wave));
     }
     if (h->d_snap) n_chunks = 1;
     n_chunks = std::min(n_chunks, std::min(h->grid, 64));
     h->last_chunks = n_chunks;
+    FsArgsHost a;
+    fill_args(h, a);
+    void *args[] = {&a};
+    const size_t bpw = (size_t)c.dof * c.n_slices * h->ft;
+    const unsigned long long per_launch = (unsigned long long)c.operator_runs * c.metro_steps_per_operator_run;
+    if (n_chunks == 1) {
+        // one chunk: copy in, sweeps and copy out in the handle's stream order, no events
+        const size_t bytes = (size_t)c.n_walkers * bpw;
+        CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), FS_ERR_CUDA);
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_paths, paths_in, bytes, cudaMemcpyHostToDevice, h->stream), FS_ERR_CUDA);
+        a.block_offset = 0;
+        for (int i = 0; i < n_launches; i++) {
+            a.step_base = h->steps_done + per_launch * (unsigned long long)i;
+            if (h->d_snap)
+                CUDA_TRY(h, cudaMemcpyAsync(h->d_snap, h->d_seeds, (h->n_threads + 1) * 16, cudaMemcpyDeviceToDevice,
+                                            h->stream), FS_ERR_CUDA);
+            CUDA_TRY(h, cudaLaunchKernel((const void *)h->k_metro, dim3(h->grid), dim3(h->block), args, h->smem,
+                                         h->stream), FS_ERR_LAUNCH);
+        }
+        CUDA_TRY(h, cudaMemcpyAsync(paths_out, h->d_paths, bytes, cudaMemcpyDeviceToHost, h->stream), FS_ERR_CUDA);
+        h->steps_done += per_launch * (unsigned long long)n_launches;
+        CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), FS_ERR_CUDA);
+        h->timed = true;
+        return FS_OK;
+    }
     if (!h->s_in) CUDA_TRY(h, cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking), FS_ERR_CUDA);
     if (!h->s_out) CUDA_TRY(h, cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking), FS_ERR_CUDA);
     if (!h->s_comp2) CUDA_TRY(h, cudaStreamCreateWithFlags(&h->s_comp2, cudaStreamNonBlocking), FS_ERR_CUDA);
@@ -1101,11 +1129,6 @@ extern "C" int fs_run_host(fs_handle *h, const void *paths_in, void *paths_out, 
         CUDA_TRY(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), FS_ERR_CUDA);
         h->ev_chunk.push_back(e);
     }
-    FsArgsHost a;
-    fill_args(h, a);
-    void *args[] = {&a};
-    const size_t bpw = (size_t)c.dof * c.n_slices * h->ft;
-    const unsigned long long per_launch = (unsigned long long)c.operator_runs * c.metro_steps_per_operator_run;
     CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream), FS_ERR_CUDA);
     // the copy streams start after everything queued before this call
     CUDA_TRY(h, cudaStreamWaitEvent(h->s_in, h->ev0, 0), FS_ERR_CUDA);
