@@ -53,10 +53,11 @@ __device__ __forceinline__ double fs_xs_double(FsXorshift &s)
 // top 24 bits of the difference are the new digit; an `and` clears the low byte.  Steps are
 // chained through the carry flag inside one asm block, so a step costs two instructions and
 // its critical path is one.  The borrow enters the chain as `0 - c` and leaves it as
-// `(0 - 0 - borrow) & 1`, i.e. only through subtractions, whichever polarity the flag has.
+// `0 - 0 - borrow` (so c is 0 or 0xFFFFFFFF), i.e. only through subtractions, whichever
+// polarity the flag has.
 struct FsRanlux {
     fs_u32 s[24];   // k << 8; s[0] is the reference's s01
-    fs_u32 carry;   // 0 or 1 (the reference stores 0 or 2^-24)
+    fs_u32 carry;   // 0 or 0xFFFFFFFF (the reference stores 0 or 2^-24)
     fs_u32 in24;
     fs_u32 stepnr;
     fs_u32 dummy;   // padding word of the table, carried through unchanged
@@ -71,7 +72,7 @@ __device__ __forceinline__ void fs_rl_chunk4_p0(FsRanlux &r)
         "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
         "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
         "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "}"
         : "+r"(r.s[23]), "+r"(r.s[22]), "+r"(r.s[21]), "+r"(r.s[20]), "+r"(r.carry)
         : "r"(r.s[9]), "r"(r.s[8]), "r"(r.s[7]), "r"(r.s[6]));
 }
@@ -83,7 +84,7 @@ __device__ __forceinline__ void fs_rl_chunk4_p4(FsRanlux &r)
         "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
         "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
         "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "}"
         : "+r"(r.s[19]), "+r"(r.s[18]), "+r"(r.s[17]), "+r"(r.s[16]), "+r"(r.carry)
         : "r"(r.s[5]), "r"(r.s[4]), "r"(r.s[3]), "r"(r.s[2]));
 }
@@ -95,7 +96,7 @@ __device__ __forceinline__ void fs_rl_chunk4_p8(FsRanlux &r)
         "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
         "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
         "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "}"
         : "+r"(r.s[15]), "+r"(r.s[14]), "+r"(r.s[13]), "+r"(r.s[12]), "+r"(r.carry)
         : "r"(r.s[1]), "r"(r.s[0]), "r"(r.s[23]), "r"(r.s[22]));
 }
@@ -107,7 +108,7 @@ __device__ __forceinline__ void fs_rl_chunk4_p12(FsRanlux &r)
         "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
         "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
         "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "}"
         : "+r"(r.s[11]), "+r"(r.s[10]), "+r"(r.s[9]), "+r"(r.s[8]), "+r"(r.carry)
         : "r"(r.s[21]), "r"(r.s[20]), "r"(r.s[19]), "r"(r.s[18]));
 }
@@ -119,7 +120,7 @@ __device__ __forceinline__ void fs_rl_chunk4_p16(FsRanlux &r)
         "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
         "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
         "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "}"
         : "+r"(r.s[7]), "+r"(r.s[6]), "+r"(r.s[5]), "+r"(r.s[4]), "+r"(r.carry)
         : "r"(r.s[17]), "r"(r.s[16]), "r"(r.s[15]), "r"(r.s[14]));
 }
@@ -131,7 +132,7 @@ __device__ __forceinline__ void fs_rl_chunk4_p20(FsRanlux &r)
         "subc.cc.u32 %1, %6, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
         "subc.cc.u32 %2, %7, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
         "subc.cc.u32 %3, %8, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "and.b32 %4, %4, 1;\n\t}"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %4, fsz, fsz;\n\t" "}"
         : "+r"(r.s[3]), "+r"(r.s[2]), "+r"(r.s[1]), "+r"(r.s[0]), "+r"(r.carry)
         : "r"(r.s[13]), "r"(r.s[12]), "r"(r.s[11]), "r"(r.s[10]));
 }
@@ -163,7 +164,7 @@ __device__ __forceinline__ void fs_rl_cycle(FsRanlux &r)
         "subc.cc.u32 %2, %12, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
         "subc.cc.u32 %1, %11, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
         "subc.cc.u32 %0, %10, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "and.b32 %24, %24, 1;\n\t}"
+        "mov.u32 fsz, 0;\n\t" "subc.u32 %24, fsz, fsz;\n\t" "}"
         : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
 }
 
@@ -274,7 +275,7 @@ __device__ __forceinline__ void fs_rl_seed(FsRanlux &r, fs_u64 x)
     }
     r.in24 = 0u;
     r.stepnr = 0u;
-    r.carry = r.s[23] == 0u ? 1u : 0u;
+    r.carry = r.s[23] == 0u ? 0xFFFFFFFFu : 0u;
     r.dummy = 0u;
 #pragma unroll 1
     for (int i = 0; i < 32; i++) fs_rl_cycle(r);
@@ -285,7 +286,7 @@ __device__ __forceinline__ void fs_rl_load(FsRanlux &r, const fs_u32 *t)
 {
 #pragma unroll
     for (int i = 0; i < 24; i++) r.s[i] = (fs_u32)__fmul_rn(__uint_as_float(t[i]), 4294967296.0f);
-    r.carry = t[24] != 0u ? 1u : 0u;
+    r.carry = t[24] != 0u ? 0xFFFFFFFFu : 0u;
     r.dummy = t[25];
     r.in24 = t[26];
     r.stepnr = t[27];
