@@ -627,11 +627,11 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     h->n_threads = (long long)c.n_walkers * h->tpw;
     h->ft = c.enable_double ? 8 : 4;
     {
-        // float-float correlator sums (FP64 / Kahan modes, FP32 builds) with at most 4 lags per
-        // thread run every lag in one pass over the slice values, stored twice in a row so
-        // that slice s1 + tau needs no wrap
+        // float-float correlator sums (every mode but the reference's FP32 order, FP32 builds)
+        // with at most 4 lags per thread run every lag in one pass over the slice values,
+        // stored twice in a row so that slice s1 + tau needs no wrap
         const long long lpt = (c.n_slices / 2 + h->tpw - 1) / h->tpw;
-        h->cor_ilv = ((c.accum == 1 || c.accum == 2) && !c.enable_double && lpt <= 4) ? 1 : 0;
+        h->cor_ilv = (c.accum != 0 && !c.enable_double && lpt <= 4) ? 1 : 0;
         // per-walker stride an odd multiple of 64 bytes: two walkers sharing a warp read
         // opposite bank halves
         const long long q = 64 / (long long)h->ft;

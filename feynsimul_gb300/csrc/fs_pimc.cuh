@@ -27,12 +27,13 @@
 #define FS_LPT ((FS_HALF_N + FS_TPW - 1) / FS_TPW)  // correlator lags owned per thread
 #define FS_COR_REGS (FS_ACCUM != 3 && FS_LPT * FS_NCOR <= 16)
 #define FS_CSTEP (FS_N % 4 == 0 ? 4 : 1)  // FP64 correlator: partial sums over s1 mod 4
-// Correlator sums of the FP64 and Kahan modes in FP32 builds: float-float per measurement
-// (fs_ff_add), then one FP64 add per lag.  FS_COR_ILV (set by the host, which sizes shared
-// memory for it): a thread owning at most 4 lags sums them in one pass over the slice values,
-// which are stored twice in a row (FS_CSTRIDE = 2N words per correlator) so that slice
-// s1 + tau is read without a wrap.
-#define FS_COR_FF ((FS_ACCUM == 1 || FS_ACCUM == 2) && !FS_DOUBLE)
+// Correlator FP64 sums of FP32 builds (FP64, Kahan and study modes): float-float per
+// measurement (fs_ff_add), then one FP64 add per lag; the study's FP32 and Kahan columns sum
+// the same products in slice order.  FS_COR_ILV (set by the host, which sizes shared memory
+// for it): a thread owning at most 4 lags sums them in one pass over the slice values, which
+// are stored twice in a row (FS_CSTRIDE = 2N words per correlator) so that slice s1 + tau is
+// read without a wrap.
+#define FS_COR_FF (FS_ACCUM != 0 && !FS_DOUBLE)
 #ifndef FS_COR_ILV
 #define FS_COR_ILV 0
 #endif
@@ -759,19 +760,42 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                 // every lag this thread owns in one pass over the slices: 2 x FS_LPT independent
                 // float-float chains, and Cc[s1] loaded once for all lags.  Unrolled by 8 (HO,
                 // N=128, 4 lags: 0.78 / 0.61 / 0.53 / 0.47 ms per launch for 1 / 2 / 4 / 8;
-                // a full unroll, 0.81 ms, misses the instruction cache).  Lags past N/2 (when
+                // a full unroll, 0.81 ms, misses the instruction cache); by 2 in the study mode,
+                // whose three sums per product make the loop body large (10-atom cluster: 2.08
+                // against 1.80-1.87e9 node updates/s at 8).  Lags past N/2 (when
                 // FS_TPW does not divide N/2) are summed and dropped; s1 + tau < N + LPT * TPW
                 // <= 2N stays inside the doubled slice values.
                 {
                     float fs[FS_LPT], fe[FS_LPT];
+#if FS_ACCUM == 3
+                    float af[FS_LPT], aks[FS_LPT], akc[FS_LPT];
+#endif
 #pragma unroll
-                    for (int j = 0; j < FS_LPT; j++) { fs[j] = 0.0f; fe[j] = 0.0f; }
+                    for (int j = 0; j < FS_LPT; j++) {
+                        fs[j] = 0.0f;
+                        fe[j] = 0.0f;
+#if FS_ACCUM == 3
+                        const int tau = t + j * FS_TPW;
+                        const FsCorAcc a0 = tau < FS_HALF_N ? g_cor[c * FS_HALF_N + tau] : FsCorAcc{};
+                        af[j] = a0.f; aks[j] = a0.ks; akc[j] = a0.kc;
+#endif
+                    }
+#if FS_ACCUM == 3
+#pragma unroll 2
+#else
 #pragma unroll 8
+#endif
                     for (int s1 = 0; s1 < FS_N; s1++) {
                         const FT c0 = Cc[s1];
 #pragma unroll
-                        for (int j = 0; j < FS_LPT; j++)
-                            fs_ff_add(fs[j], fe[j], FS_MUL(c0, Cc[s1 + t + j * FS_TPW]));
+                        for (int j = 0; j < FS_LPT; j++) {
+                            const FT q = FS_MUL(c0, Cc[s1 + t + j * FS_TPW]);
+                            fs_ff_add(fs[j], fe[j], q);
+#if FS_ACCUM == 3
+                            af[j] = __fadd_rn(af[j], q);
+                            fs_kahan(aks[j], akc[j], q);
+#endif
+                        }
                     }
 #pragma unroll
                     for (int j = 0; j < FS_LPT; j++) {
@@ -780,7 +804,15 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                         cacc[c][j] = __dadd_rn(cacc[c][j], m);
 #else
                         const int tau = t + j * FS_TPW;
-                        if (tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = __dadd_rn(g_cor[c * FS_HALF_N + tau], m);
+                        if (tau < FS_HALF_N) {
+#if FS_ACCUM == 3
+                            FsCorAcc *g = g_cor + c * FS_HALF_N + tau;
+                            g->d = __dadd_rn(g->d, m);
+                            g->f = af[j]; g->ks = aks[j]; g->kc = akc[j];
+#else
+                            g_cor[c * FS_HALF_N + tau] = __dadd_rn(g_cor[c * FS_HALF_N + tau], m);
+#endif
+                        }
 #endif
                     }
                 }
@@ -802,9 +834,19 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                     {
                         float fs = 0.0f, fe = 0.0f;
 #pragma unroll 4
-                        for (int s1 = 0; s1 < FS_N; s1++)
-                            fs_ff_add(fs, fe, FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]));
+                        for (int s1 = 0; s1 < FS_N; s1++) {
+                            const FT q = FS_MUL(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)]);
+                            fs_ff_add(fs, fe, q);
+#if FS_ACCUM == 3
+                            acc.f = __fadd_rn(acc.f, q);
+                            fs_kahan(acc.ks, acc.kc, q);
+#endif
+                        }
+#if FS_ACCUM == 3
+                        acc.d = __dadd_rn(acc.d, __dadd_rn(fs_f2d(fs), fs_f2d(fe)));
+#else
                         acc = __dadd_rn(acc, __dadd_rn(fs_f2d(fs), fs_f2d(fe)));
+#endif
                     }
 #elif FS_ACCUM == 0 && FS_PARALLEL
                     // the reference's summation order (kernel.c:736-793)

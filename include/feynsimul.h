@@ -202,7 +202,10 @@ int fs_sync_timeout(fs_handle *h, double seconds);
  * FS_ACCUM_STUDY: plain FP32, Kahan FP32, FP64 sums of the same values), returned as
  * double.  Correlator: [walkers][n_corr][N/2] running sums since creation / the last
  * fs_zero_accumulators, as double; FS_ACCUM_STUDY: [..][4] = plain FP32 sum, Kahan sum,
- * Kahan compensation, FP64 sum.  Bins: [res^DOF] counts.  Histogram: [hist_bins] counts. */
+ * Kahan compensation, FP64 sum.  In FP32 builds every mode but FS_ACCUM_REF_FP32 sums one
+ * measurement's products of a lag in float-float (about 48 significant bits) before adding
+ * them to the lag's FP64 running sum.  Bins: [res^DOF] counts.  Histogram: [hist_bins]
+ * counts. */
 int fs_get_operators(fs_handle *h, double *out, size_t n);
 int fs_get_correlator(fs_handle *h, double *out, size_t n);
 /* Per-walker operator means [n_ops][walkers]: each walker's thread means averaged on the

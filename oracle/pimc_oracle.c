@@ -268,9 +268,10 @@ static inline void fso_kahan_add(fso_kahan_t *k, float x)
  * a lag are summed in float-float -- Knuth's TwoSum gives the rounding error of every add
  * exactly, and the errors are summed on the side (Ogita, Rump and Oishi, "Accurate sum and
  * dot product", SIAM J. Sci. Comput. 26 (2005), Algorithm 4.4 "Sum2") -- and s + e joins the
- * lag's FP64 running sum.  The error of the measurement's sum is bounded by about
- * N * 2^-48 * sum |products|, far below the FP32 rounding of the products themselves. */
-#define FSO_COR_FF ((FS_ACCUM == 1 || FS_ACCUM == 2) && !FS_DOUBLE)
+ * lag's FP64 running sum (the study's FP64 column likewise; its FP32 and Kahan columns
+ * sum the same products in slice order).  The error of the measurement's sum is bounded by
+ * about N * 2^-48 * sum |products|, far below the FP32 rounding of the products themselves. */
+#define FSO_COR_FF (FS_ACCUM != 0 && !FS_DOUBLE)
 static inline void fso_ff_add(float *s, float *e, float q)
 {
     const float t = *s + q;
@@ -527,8 +528,14 @@ int fso_run(fso_args_t *A)
 #elif FSO_COR_FF
                     {
                         float fs = 0.0f, fe = 0.0f;
-                        for (uint32_t s1 = 0; s1 < FS_N; s1++)
-                            fso_ff_add(&fs, &fe, fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c));
+                        for (uint32_t s1 = 0; s1 < FS_N; s1++) {
+                            const FT pr = fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
+                            fso_ff_add(&fs, &fe, pr);
+#if FS_ACCUM == 3
+                            cor32[c][tau] = cor32[c][tau] + (float)pr;
+                            fso_kahan_add(&cork[c][tau], (float)pr);
+#endif
+                        }
                         cord[c][tau] = cord[c][tau] + ((double)fs + (double)fe);
                     }
 #else
@@ -560,8 +567,14 @@ int fso_run(fso_args_t *A)
             for (int c = 0; c < FS_NCOR; c++)
                 for (int tau = 0; tau < FS_HALF_N; tau++) {
                     float fs = 0.0f, fe = 0.0f;
-                    for (uint32_t s1 = 0; s1 < FS_N; s1++)
-                        fso_ff_add(&fs, &fe, fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c));
+                    for (uint32_t s1 = 0; s1 < FS_N; s1++) {
+                        const FT pr = fso_cor_prod(path, s1, (s1 + (uint32_t)tau) % FS_N, c);
+                        fso_ff_add(&fs, &fe, pr);
+#if FS_ACCUM == 3
+                        cor32[c][tau] = cor32[c][tau] + (float)pr;
+                        fso_kahan_add(&cork[c][tau], (float)pr);
+#endif
+                    }
                     cord[c][tau] = cord[c][tau] + ((double)fs + (double)fe);
                 }
 #else

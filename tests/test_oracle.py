@@ -4,7 +4,7 @@ present, against the reference built live (oracle/build_ref.py)."""
 import numpy as np
 import pytest
 
-from golden_cases import load_ranlux, load_sweep, oracle_config, sweep_cases
+from golden_cases import HO, load_ranlux, load_sweep, oracle_config, sweep_cases
 from oracle import oracle as orc
 
 
@@ -94,10 +94,10 @@ def test_oracle_against_live_reference():
 @pytest.mark.parametrize("case", ["xorshift_walker", "xorshift_parallel"])
 def test_oracle_study_correlator_columns(case):
     """Precision-study accumulation sums the same products three ways on one trajectory:
-    its FP64 column holds plain FP64 sums, which the FP64 mode's float-float sums per
-    measurement (about 48 significant bits, then FP64) match to 1e-12 relative; in walker
-    mode (where the FP32 mode also adds slices in ascending order) its plain-FP32 column
-    equals the FP32 mode's sums bit for bit; the Kahan column lies between in error."""
+    its FP64 column (float-float per measurement, then FP64) equals the FP64 mode's sums bit
+    for bit, and in walker mode (where the FP32 mode also adds slices in ascending order) its
+    plain-FP32 column equals the FP32 mode's sums bit for bit; the Kahan column lies between
+    in error."""
     ka, _ = load_sweep(case)
     rng = np.random.RandomState(5)
     outs = {}
@@ -115,9 +115,7 @@ def test_oracle_study_correlator_columns(case):
         outs[accum] = o
     st = outs[3].cor_means
     assert np.array_equal(outs[3].paths, outs[1].paths)
-    scale = np.abs(st["d"]).max()
-    assert np.abs(outs[1].cor_means - st["d"]).max() <= 1e-12 * scale
-    assert not np.array_equal(outs[1].cor_means, outs[3].cor_means["f"].astype(np.float64))
+    assert np.array_equal(st["d"], outs[1].cor_means)
     if not ka["enableParallelizePath"]:
         assert np.array_equal(st["f"], outs[0].cor_means)
     ref = st["d"]
@@ -125,6 +123,38 @@ def test_oracle_study_correlator_columns(case):
     err_k = np.abs(st["ks"].astype(np.float64) - ref).max()
     assert err_k <= err_f + 1e-12
     assert err_f <= 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("parallel", [True, False], ids=["parallel", "walker"])
+def test_oracle_correlator_sums_against_exact(parallel):
+    """One sweep, then one measurement: each lag's correlator sum comes from the final path
+    alone, so it is checked against the exact sum (math.fsum) of the same FP32 products.
+    The FP64 column (float-float per measurement, then FP64) stays within N * 2^-48 * sum|q|
+    of it; the plain FP32 column is typically ~1e3 times further off."""
+    import math
+    W, N, S = 8, 64, 3
+    cfg = orc.OracleConfig(DOF=1, potential=HO["potential"], userCode=HO["userCode"], nbrOfWalkers=W, N=N,
+                           beta=10.0, S=S, operatorRuns=1, metroStepsPerOperatorRun=1,
+                           enableParallelizePath=parallel, operators=("x1 * x1",), correlators=("x1",),
+                           accum=3)
+    o = orc.OracleSampler(cfg)
+    rng = np.random.RandomState(11)
+    o.paths[...] = (rng.randn(*o.paths.shape) * 10 ** rng.uniform(-2, 2, size=o.paths.shape)).astype(np.float32)
+    o.seeds[...] = rng.randint(0, 2 ** 31 - 1, size=o.seeds.shape).astype(np.uint32)
+    o.walker_seeds[...] = rng.randint(0, 2 ** 31 - 1, size=o.walker_seeds.shape).astype(np.uint32)
+    o.run()
+    x = o.paths.reshape(W, N).astype(np.float32)
+    st = o.cor_means.reshape(W, N // 2)
+    worst_d = worst_f = 0.0
+    for w in range(W):
+        for tau in range(N // 2):
+            q = (x[w] * np.roll(x[w], -tau)).astype(np.float64)   # FP32 products, exactly in FP64
+            exact = math.fsum(q)
+            scale = float(np.abs(q).sum())
+            assert abs(st["d"][w, tau] - exact) <= N * 2.0 ** -48 * scale
+            worst_d = max(worst_d, abs(st["d"][w, tau] - exact) / scale)
+            worst_f = max(worst_f, abs(float(st["f"][w, tau]) - exact) / scale)
+    assert worst_d < 1e-3 * worst_f
 
 
 def _golden_lm2m2():
