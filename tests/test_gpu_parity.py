@@ -102,6 +102,11 @@ FIXED_CASES = {
     "xorshift_walker_snm_only": {},
     "ranlux_walker_moves": {},
     "xorshift_walker_shift_double": {},
+    # edge geometries of the correlator sums: one lag per thread; one thread per walker
+    # owning 4 lags; walker mode whose 4 lags take the one-pass loop
+    "xorshift_parallel:n4_s1": dict(N=4, S=1),
+    "xorshift_parallel:n8_s3": dict(N=8, S=3),
+    "xorshift_walker:n8": dict(N=8),
 }
 
 
@@ -118,7 +123,7 @@ def _oracle_correlator(o, accum):
 @pytest.mark.parametrize("accum", [1, 0, 2, 3])
 def test_fixed_mode_matches_oracle(case, accum, global_path):
     from oracle import oracle as orc
-    ka, rec = load_sweep(case)
+    ka, rec = load_sweep(case.split(":")[0])
     ka = dict(ka, enableGlobalPath=global_path, **FIXED_CASES[case])
     accname = {0: "fp32", 1: "fp64", 2: "kahan", 3: "study"}[accum]
     k = kernel_for_case(ka, compat=False, accumulation=accname, fast=False)
