@@ -399,8 +399,13 @@ def batch_bench(args):
     for _ in range(max(3, args.warmup)):
         b.run(1)
     steps = max(3, min(args.steps, 10))
+    import torch
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
     t = b.run(steps, graph=True)
+    clk = clocks.stop()
     value = b.node_updates_per_launch * steps / t
+    path_bytes = sum(w["walkers"] * w["N"] * 3 * (w["n"] - 1) * 4 for w in wl)
     # algorithmic lane operations of one launch: per system, node updates x (xorshift 8 per
     # uniform x 2 DOF uniforms + Box-Muller 9 per DOF + two LM2M2 cluster evaluations)
     ops = 0.0
@@ -408,7 +413,7 @@ def batch_bench(args):
         n, dof = w["n"], 3 * (w["n"] - 1)
         nodes = w["walkers"] * (w["N"] >> sy.bisection_level) * ((1 << sy.bisection_level) - 1) * 4
         ops += nodes * (16 * dof + 9 * dof + 2 * lm2m2_cluster_ops(n))
-    clk_mhz = 2070.0
+    clk_mhz = clk.get("sm_mhz") or 2070.0
     peak = 4 * 32 * 152 * clk_mhz * 1e6 / 1e12
     achieved = ops * steps / t / 1e12
     out = {"metric": "path-node updates/s, ragged batch of 64 LM2M2 systems in one persistent launch",
@@ -419,7 +424,9 @@ def batch_bench(args):
                            "xorshift, 4 sweeps + 1 energy measurement per step",
                "node_updates_per_step": b.node_updates_per_launch, "work_items": b.n_items, "grid": b.grid,
                "block_threads": tune["block_threads"], "tpw_target": tune["tpw_target"],
-               "registers": b.registers, "smem_bytes": b.smem, "cuda_graph": True},
+               "registers": b.registers, "smem_bytes": b.smem, "cuda_graph": True,
+               "l2": f"inputs larger than L2 ({path_bytes / 1e9:.1f} GB of paths)"},
+           "clocks": clk,
            "autotune": {"cached": tune["cached"], "seconds": t_tune,
                         "candidates": [{k: c.get(k) for k in ("block_threads", "tpw_target", "node_updates_per_s",
                                                               "error")} for c in tune.get("candidates", [])]},
@@ -427,9 +434,58 @@ def batch_bench(args):
            "roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
                         "frac": achieved / peak, "traffic": None,
                         "alg_ops_per_node": ops / b.node_updates_per_launch,
-                        "peak_basis": "4 x 32 x 152 lanes per clock at 2070 MHz"}}
+                        "peak_basis": f"4 x 32 x 152 lanes per clock at {clk_mhz:.0f} MHz"}}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = batch_cpu_rate(wl, b, seconds=args.cpu_seconds)
     b.close()
     return out
+
+
+def batch_cpu_rate(wl, b, seconds=10.0, walkers=16):
+    """Node updates/s of the oracle's C restatement on the host cores for the ragged batch:
+    every system run on its own (a subset of walkers, the batch's N, S, T and cadence), each
+    system's CPU time per node update weighted by its node updates in the full workload."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as orc
+    cores = cpu_cores()
+    cfgs = []
+    for w, sy in zip(wl, b.systems):
+        c = b.clusters[w["n"]]
+        W = min(walkers, w["walkers"])
+        cfgs.append(orc.OracleConfig(
+            DOF=c.DOF, potential=c.potential, userCode=c.userCode, nbrOfWalkers=W, N=w["N"], beta=1.0 / w["T"],
+            S=sy.bisection_level, operatorRuns=1, metroStepsPerOperatorRun=4, enableParallelizePath=True,
+            operators=(c.energyOp,), compat=False, accum=1))
+    with ThreadPoolExecutor(max_workers=cores) as ex:      # gcc runs in subprocesses
+        list(ex.map(orc.build, cfgs))
+    per_node, real_nodes, sample_nodes, sample_t = [], [], 0, 0.0
+    budget = seconds / len(cfgs)
+    for w, sy, cfg in zip(wl, b.systems, cfgs):
+        c = b.clusters[w["n"]]
+        o = orc.OracleSampler(cfg, omp_threads=cores)
+        o.paths[...] = c.initial_paths(cfg.nbrOfWalkers, w["N"], np.random.RandomState(1)).astype(np.float32)
+        rs = np.random.RandomState(2)
+        o.seeds[...] = rs.randint(0, 2 ** 31 - 1, size=o.seeds.shape)
+        o.walker_seeds[...] = rs.randint(0, 2 ** 31 - 1, size=o.walker_seeds.shape)
+        seg = 2 ** sy.bisection_level
+        nodes_launch = cfg.nbrOfWalkers * (w["N"] // seg) * (seg - 1) * 4
+        runs, dt = 0, 0.0
+        while runs < 1 or (dt < budget and runs < 1000):
+            t0 = time.perf_counter()
+            o.run()
+            dt += time.perf_counter() - t0
+            runs += 1
+        per_node.append(dt / (runs * nodes_launch))
+        real_nodes.append(w["walkers"] * (w["N"] // seg) * (seg - 1) * 4)
+        sample_nodes += runs * nodes_launch
+        sample_t += dt
+    total_nodes = float(np.sum(real_nodes))
+    value = total_nodes / float(np.dot(real_nodes, per_node))
+    return {"value": value, "unit": "node-updates/s", "cores": cores, "kind": "port",
+            "sample": f"each of the {len(cfgs)} systems with {walkers} walkers, its N, S, T and cadence "
+                      f"({sample_nodes} node updates, {sample_t:.1f} s); per-system CPU time per node update "
+                      f"weighted by the system's node updates in the full workload; oracle C restatement, "
+                      f"OpenMP over walkers"}
 
 
 def lm2m2_cluster_ops(n):
@@ -453,14 +509,20 @@ def precision_bench(args):
         kw["op_runs"] = args.op_runs
     if args.msteps:
         kw["msteps"] = args.msteps
+    import torch
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()        # sampled over the whole study: both arms' timed launches are inside
     r = precision_study(launches=max(2, args.steps), log=lambda m: print(m, file=sys.stderr), **kw)
+    clk = clocks.stop()
     dof = 27
     per_node = 16 * dof + 9 * dof + 2 * lm2m2_cluster_ops(10)
-    peak = 4 * 32 * 152 * 2070.0 * 1e6 / 1e12
+    clk_mhz = clk.get("sm_mhz") or 2070.0
+    peak = 4 * 32 * 152 * clk_mhz * 1e6 / 1e12
     achieved = r["fp32_node_updates_per_s"] * per_node / 1e12
     return {"roofline": {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
                          "frac": achieved / peak, "traffic": None, "alg_ops_per_node": per_node,
-                         "peak_basis": "4 x 32 x 152 lanes per clock at 2070 MHz (FP32 arm)"},
+                         "peak_basis": f"4 x 32 x 152 lanes per clock at {clk_mhz:.0f} MHz (FP32 arm)"},
+            "clocks": clk,
             "metric": "precision study: FP32-path error vs FP64-everywhere, per result",
             "value": r["fp32_node_updates_per_s"], "unit": "node-updates/s (FP32 path, study sums)",
             "n_gpus": 1, "higher_is_better": True, "dtype": "f32 path, f64/f32/kahan sums",
