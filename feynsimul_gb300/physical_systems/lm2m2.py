@@ -191,6 +191,119 @@ def jacobi_matrix(n: int, m: float) -> np.ndarray:
     return J
 
 
+def _set_cluster_code(obj, n: int, J: np.ndarray, reference_derivative: bool,
+                      length_A: float = 1.0, v_scale: float = 1.0) -> None:
+    """Plugin code of n LM2M2 atoms in Jacobi coordinates xi = J r.
+
+    Sets obj.J, obj.B (positions relative to the centre of mass from the relative xi),
+    obj.pairs, obj.userCode, obj.potential, obj.energyOp (virial energy),
+    obj.meanSquaredRadiusOp (sum of squared pair distances [Angstrom^2]) and
+    obj.pairDistanceOps (pair distances [Angstrom]).  Coordinates are in units of length_A
+    Angstrom; the potential and the energy are v_scale times their value in Kelvin."""
+    dof = 3 * (n - 1)
+    obj.J = J
+    obj.B = np.linalg.inv(J)[:, : n - 1]
+    obj.pairs = [(a, b) for a in range(n) for b in range(a + 1, n)]
+    BA = obj.B * length_A                 # positions in Angstrom
+    xs = [f"x{i + 1}" for i in range(dof)]
+    args = ", ".join(f"FLOAT_TYPE {v}" for v in xs)
+
+    def comp(coefs, dim):
+        terms = [f"{float(c)!r} * {xs[3 * k + dim]}" for k, c in enumerate(coefs) if abs(c) > 1e-15]
+        return " + ".join(terms) if terms else "0.0"
+
+    # positions relative to the centre of mass, then pair sums
+    pos = []
+    for a in range(n):
+        for dim in range(3):
+            pos.append(f"    FLOAT_TYPE p{a}_{dim} = {comp(BA[a], dim)};")
+    r2 = {}
+    for (a, b) in obj.pairs:
+        r2[(a, b)] = " + ".join(f"fs_sq(p{a}_{dim} - p{b}_{dim})" for dim in range(3))
+    body_pos = "\n".join(pos)
+    pot_sum = " + ".join(f"lm2m2_r2({r2[p]})" for p in obj.pairs)
+    vir_terms = []
+    for i, p in enumerate(obj.pairs):
+        vir_terms.append(f"    {{ FLOAT_TYPE q = {r2[p]}; e += lm2m2_r2(q) + q * dlm2m2_dr2(q); }}")
+    msr = " + ".join(r2[p] for p in obj.pairs)
+    scaled = (lambda e: e) if v_scale == 1.0 else (lambda e: f"{v_scale!r} * ({e})")
+    obj.userCode = lm2m2_c_code(reference_derivative) + f"""
+inline FLOAT_TYPE lm2m2_cluster_potential({args})
+{{
+{body_pos}
+    return {scaled(pot_sum)};
+}}
+inline FLOAT_TYPE lm2m2_cluster_virial_energy({args})
+{{
+{body_pos}
+    FLOAT_TYPE e = 0.0;
+{chr(10).join(vir_terms)}
+    return {scaled("e")};
+}}
+inline FLOAT_TYPE lm2m2_cluster_pair_r2_sum({args})
+{{
+{body_pos}
+    return {msr};
+}}
+"""
+    call = ", ".join(xs)
+    obj.potential = f"lm2m2_cluster_potential({call})"
+    obj.energyOp = f"lm2m2_cluster_virial_energy({call})"
+    obj.meanSquaredRadiusOp = f"lm2m2_cluster_pair_r2_sum({call})"
+    obj.pairDistanceOps = tuple(
+        "sqrt(" + " + ".join(
+            f"fs_sq({comp(BA[a] - BA[b], dim)})" for dim in range(3)) + ")"
+        for (a, b) in obj.pairs)
+
+
+# Kelvin in electronvolts as the reference's pair-potential routines use it
+# (lm2m2_3part.py userCode, lm2m2_4part.py userCode: k = 8.6173324e-5 eV/K)
+KB_EV = 8.6173324e-5
+
+
+def reference_helper_code(eV_per_unit=None) -> str:
+    """C helpers under the names the reference's plugins define, for operator strings written
+    against them: sqr; lm2m2sqrt(r^2) [K] and dlm2m2sqrtdr(r^2) = d/d(r^2) (lm2m2.h:17-147);
+    with ``eV_per_unit`` also lm2m2(r) and dlm2m2dr(r) = d/dr in eV for r in Angstrom (the
+    three- and four-atom plugins' userCode).  Requires lm2m2_c_code's functions."""
+    code = """
+inline FLOAT_TYPE sqr(FLOAT_TYPE v) { return v * v; }
+inline FLOAT_TYPE lm2m2sqrt(FLOAT_TYPE sr) { return lm2m2_r2(sr); }
+inline FLOAT_TYPE dlm2m2sqrtdr(FLOAT_TYPE sr) { return dlm2m2_dr2(sr); }
+"""
+    if eV_per_unit is not None:
+        code += f"""inline FLOAT_TYPE lm2m2(FLOAT_TYPE r) {{ return {KB_EV!r} * lm2m2_r2(r * r); }}
+inline FLOAT_TYPE dlm2m2dr(FLOAT_TYPE r) {{ return {2.0 * KB_EV!r} * r * dlm2m2_dr2(r * r); }}
+"""
+    return code
+
+
+def _set_unit_cluster(obj, n: int, angstrom_per_unit: float, eV_per_unit: float,
+                      reference_derivative: bool) -> None:
+    """n atoms in the units of the reference's three- and four-atom plugins: hbar = m_He = 1,
+    so the coordinates are Jacobi vectors of unit masses, in units of angstrom_per_unit
+    Angstrom, and the potential is in units of 1 / eV_per_unit eV.  Sets the plugin code and
+    the reference's operators (lm2m2_3part.py:26-28, lm2m2_4part.py:31-33): mean squared
+    radius and mean radius about the centre of mass, and mean squared pair distance, all in
+    coordinate units."""
+    _set_cluster_code(obj, n, jacobi_matrix(n, 1.0), reference_derivative,
+                      length_A=angstrom_per_unit, v_scale=KB_EV * eV_per_unit)
+    obj.pairR2SumOp = obj.meanSquaredRadiusOp            # sum of squared pair distances [A^2]
+    obj.userCode += reference_helper_code(eV_per_unit)
+    xs = [f"x{i + 1}" for i in range(obj.DOF)]
+    sumsq = " + ".join(f"sqr({v})" for v in xs)
+    # unit masses: sum_a |p_a - centre|^2 = |xi|^2, and sum over pairs |p_a - p_b|^2 = n |xi|^2
+    obj.meanSquaredRadiusOp = f"{1.0 / n!r} * ({sumsq})"
+    obj.meanSquaredAtomDistOp = f"{2.0 / (n - 1)!r} * ({sumsq})"
+
+    def comp(coefs, dim):
+        terms = [f"{float(c)!r} * {xs[3 * k + dim]}" for k, c in enumerate(coefs) if abs(c) > 1e-15]
+        return " + ".join(terms) if terms else "0.0"
+
+    radii = [f"sqrt({' + '.join(f'sqr({comp(obj.B[a], dim)})' for dim in range(3))})" for a in range(n)]
+    obj.meanRadiusOp = f"{1.0 / n!r} * ({' + '.join(radii)})"
+
+
 class Lm2m2Cluster:
     """n helium-4 atoms at temperature T [K] with the LM2M2 pair potential."""
 
@@ -207,60 +320,7 @@ class Lm2m2Cluster:
         self.m = HE_MASS * self.rUnit ** 2 / HBAR ** 2 * self.potentialUnit
         if 3 <= n <= 10:
             self.groundStateEnergy = -GROUND_STATES[n - 3]
-        J = jacobi_matrix(n, self.m)
-        self.J = J
-        Jinv = np.linalg.inv(J)
-        self.B = Jinv[:, : n - 1]  # position (relative to the centre) from the relative xi
-        self.pairs = [(a, b) for a in range(n) for b in range(a + 1, n)]
-        xs = [f"x{i + 1}" for i in range(self.DOF)]
-        args = ", ".join(f"FLOAT_TYPE {v}" for v in xs)
-
-        def comp(coefs, dim):
-            terms = [f"{float(c)!r} * {xs[3 * k + dim]}" for k, c in enumerate(coefs) if abs(c) > 1e-15]
-            return " + ".join(terms) if terms else "0.0"
-
-        # positions relative to the centre of mass, then pair sums
-        pos = []
-        for a in range(n):
-            for dim in range(3):
-                pos.append(f"    FLOAT_TYPE p{a}_{dim} = {comp(self.B[a], dim)};")
-        r2 = {}
-        for (a, b) in self.pairs:
-            r2[(a, b)] = " + ".join(f"fs_sq(p{a}_{dim} - p{b}_{dim})" for dim in range(3))
-        body_pos = "\n".join(pos)
-        pot_sum = " + ".join(f"lm2m2_r2({r2[p]})" for p in self.pairs)
-        vir_terms = []
-        for i, p in enumerate(self.pairs):
-            vir_terms.append(f"    {{ FLOAT_TYPE q = {r2[p]}; e += lm2m2_r2(q) + q * dlm2m2_dr2(q); }}")
-        msr = " + ".join(r2[p] for p in self.pairs)
-        self.userCode = lm2m2_c_code(referenceDerivative) + f"""
-inline FLOAT_TYPE lm2m2_cluster_potential({args})
-{{
-{body_pos}
-    return {pot_sum};
-}}
-inline FLOAT_TYPE lm2m2_cluster_virial_energy({args})
-{{
-{body_pos}
-    FLOAT_TYPE e = 0.0;
-{chr(10).join(vir_terms)}
-    return e;
-}}
-inline FLOAT_TYPE lm2m2_cluster_pair_r2_sum({args})
-{{
-{body_pos}
-    return {msr};
-}}
-"""
-        call = ", ".join(xs)
-        self.potential = f"lm2m2_cluster_potential({call})"
-        self.energyOp = f"lm2m2_cluster_virial_energy({call})"
-        self.meanSquaredRadiusOp = f"lm2m2_cluster_pair_r2_sum({call})"
-        # pair distances [Angstrom], one expression per pair (histogram input)
-        self.pairDistanceOps = tuple(
-            "sqrt(" + " + ".join(
-                f"fs_sq({comp(self.B[a] - self.B[b], dim)})" for dim in range(3)) + ")"
-            for (a, b) in self.pairs)
+        _set_cluster_code(self, n, jacobi_matrix(n, self.m), referenceDerivative)
 
     # ---- coordinates -------------------------------------------------------------
     def positions_to_jacobi(self, r):

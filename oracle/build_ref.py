@@ -369,6 +369,33 @@ def ref_ranlux_streams(lux: int, seeds, n_calls: int, double=False):
     return out, states
 
 
+def reference_plugin_values(module: str, cls: str, attrs, x):
+    """FP64 values of expression attributes of the reference's plugin class
+    physical_systems/<module>.py:<cls> at coordinates x [m, DOF]: the class is instantiated
+    from the reference tree and its userCode and expressions are compiled as-is."""
+    import importlib.util
+    path = os.path.join(REFERENCE_ROOT, "FeynSimul", "physical_systems", module + ".py")
+    spec = importlib.util.spec_from_file_location("ref_" + module, path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    obj = getattr(mod, cls)()
+    dof = int(obj.DOF)
+    decl = " ".join(f"double x{k + 1} = x[{k}];" for k in range(dof))
+    fns = "".join(f"static double ref_f{i}(const double *x) {{ {decl} return {getattr(obj, a)}; }}\n"
+                  for i, a in enumerate(attrs))
+    calls = " ".join(f"out[(size_t)r * {len(attrs)} + {i}] = ref_f{i}(x + (size_t)r * {dof});"
+                     for i in range(len(attrs)))
+    c_text = ('#include "cl_shim.h"\n#define FLOAT_TYPE double\n' + obj.userCode + "\n" + fns +
+              "void ref_plugin_eval(const double *x, int m, double *out)\n"
+              "{ int r; for (r = 0; r < m; r++) { " + calls + " } }\n")
+    lib = ctypes.CDLL(_compile("double", c_text, f"plugin_{module}", single_constants=False))
+    lib.ref_plugin_eval.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros((x.shape[0], len(attrs)))
+    lib.ref_plugin_eval(x.ctypes.data, x.shape[0], out.ctypes.data)
+    return out
+
+
 def lm2m2_header_lib():
     """The reference's physical_systems/lm2m2.h compiled as-is: lm2m2sqrt / dlm2m2sqrtdr."""
     c_text = ('#include "cl_shim.h"\n#define FLOAT_TYPE %(FT)s\n'

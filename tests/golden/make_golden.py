@@ -11,6 +11,8 @@ RANLUXCL header on the CPU (oracle/build_ref.py) and records inputs and outputs:
   0-4 and p=124, FP32 and FP64 variants (pyopencl-ranluxcl.cl:384-557, :597-725, :893-920);
 * ``lm2m2_ref.npz``: the reference's LM2M2 pair potential and derivative routine
   (physical_systems/lm2m2.h) on a grid of pair distances;
+* ``plugins_ref.npz``: the reference's three- and four-atom plugin expressions
+  (physical_systems/lm2m2_3part.py, lm2m2_4part.py) at seeded coordinates;
 * ``sweep_<case>.npz``: initial paths and seed tables, and after each of two
   ``metropolis`` launches: paths, accept counts, seed / RANLUX tables, operator means,
   correlator sums and histogram bins (kernel.c:514-837).
@@ -134,12 +136,31 @@ def make_lm2m2():
     np.savez_compressed(os.path.join(HERE, "lm2m2_ref.npz"), **out)
 
 
+PLUGIN_ATTRS = ("potential", "energyOp", "meanSquaredRadiusOp", "meanRadiusOp", "meanSquaredAtomDistOp")
+
+
+def make_plugins():
+    """``plugins_ref.npz``: the reference's three- and four-atom LM2M2 plugins
+    (physical_systems/lm2m2_3part.py, lm2m2_4part.py): potential, virial energy operator and
+    radius operators evaluated in FP64 from their own C strings at seeded coordinates."""
+    rng = np.random.RandomState(77)
+    out = {}
+    for module, cls, dof in (("lm2m2_3part", "Lm2m2_3part", 6), ("lm2m2_4part", "Lm2m2_4part", 9)):
+        x = rng.normal(0.0, 3.0, size=(96, dof))
+        out[f"{module}_x"] = x
+        out[f"{module}_values"] = br.reference_plugin_values(module, cls, PLUGIN_ATTRS, x)
+    np.savez_compressed(os.path.join(HERE, "plugins_ref.npz"), **out)
+
+
 def main():
     if not br.reference_available():
         raise SystemExit("reference tree not present; fixtures are generated where it is")
-    make_ranlux()
-    make_lm2m2()
     only = sys.argv[1:]
+    if not only:
+        make_ranlux()
+        make_lm2m2()
+    if not only or "plugins" in only:
+        make_plugins()
     for name, ka in CASES.items():
         if only and name not in only:
             continue
