@@ -66,3 +66,26 @@ def test_few_atom_plugin_sweep_matches_oracle(module, cls, n):
     assert 0 < k.getAccepts().sum()
     assert np.all(np.isfinite(k.getOperators()))
     k.close()
+
+
+def test_three_particle_example_through_modN(tmp_path):
+    """The reference's examples/lm2m2_3particles.py set-up (its KernelArgs, plugin and
+    operators) driven through modN for a few short episodes: the files appear and the
+    energies are finite."""
+    import glob
+    from feynsimul_gb300.pimc_utils import KernelArgs, modN, read_tsv
+    from feynsimul_gb300.physical_systems.lm2m2_3part import Lm2m2_3part
+    ka = KernelArgs(nbrOfWalkers=64, N=8, enablePathShift=False, enableBisection=True, enableSingleNodeMove=False,
+                    enableGlobalPath=True, enableGlobalOldPath=True, enableParallelizePath=True, enableBins=False,
+                    enableDouble=False, enableRanlux=False, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1, beta=1000.0,
+                    nbrOfWalkersPerWorkGroup=4, operatorRuns=100, enableOperator=True, enableCorrelator=False,
+                    metroStepsPerOperatorRun=40, system=Lm2m2_3part())
+    ka.operators = (ka.system.energyOp, ka.system.meanSquaredRadiusOp, ka.system.meanRadiusOp)
+    start = np.random.RandomState(1).uniform(size=(ka.nbrOfWalkers, ka.system.DOF), low=-1.0, high=1.0) * 0.01
+    modN(ka, start, 3000, "lm2m2_3part", lambda N, S: max(2 ** 6 // 2 ** S, 1), lambda N, S: 4,
+         lambda N, S: 2, 512, finalN=16, simTime=0, resultsDir=str(tmp_path))
+    tsv = glob.glob(str(tmp_path / "lm2m2_3part" / "*" / "*" / "data.tsv"))
+    assert len(tsv) == 1
+    beta, rows, ops = read_tsv(tsv[0])
+    assert beta == 1000.0 and [r[0] for r in rows] == [8, 8, 16, 16]
+    assert ops.shape[1:] == (3, 64) and np.all(np.isfinite(ops))
