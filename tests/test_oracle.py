@@ -22,6 +22,20 @@ def test_ranlux_streams_bit_exact(lux):
         assert np.array_equal(out, g[f"f64_lux{lux}"][i])
 
 
+@pytest.mark.parametrize("lux", [0, 2, 4])
+def test_rng_moments_known_answer(lux):
+    """The reference's examples/ranlux_test.py check: uniforms with mean 1/2 and standard
+    deviation 1/sqrt(12), here on 10^6 values of the generators the golden streams pin
+    (RANLUX per luxury level, xorshift as float(w) * 2^-32), at 6 standard errors."""
+    out, _ = orc.ranlux_stream(123456789, lux, 250000)
+    xs, _ = orc.xorshift_stream([123456789, 362436069, 521288629, 88675123], 1000000)
+    for u in (out.astype(np.float64), xs.astype(np.float64) * 2.0 ** -32):
+        n = u.size
+        assert np.all((u >= 0.0) & (u < 1.0))
+        assert abs(u.mean() - 0.5) < 6 * np.sqrt(1 / 12 / n)
+        assert abs(u.std() - 1 / np.sqrt(12)) < 6 * np.sqrt(1 / 60 / n)     # Var(s) = (mu4 - s^4) / (4 s^2 n)
+
+
 def _masked(t):
     t = np.array(t).reshape(-1, 28).copy()
     t[:, 25] = 0
