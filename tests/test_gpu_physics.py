@@ -28,9 +28,9 @@ def _ho_kernel(N=64, S=3, walkers=2048, beta=8.0, op_runs=40, msteps=2, ranlux=F
     ka = kernel_args.KernelArgs(
         system=sysm, nbrOfWalkers=walkers, N=N, beta=beta, S=S, enableOperator=True,
         enableCorrelator=True, enableBisection=True, enablePathShift=False, enableSingleNodeMove=False,
-        enableBins=False, nbrOfWalkersPerWorkGroup=1, enableParallelizePath=True, enableGlobalPath=False,
-        enableGlobalOldPath=False, enableRanlux=ranlux, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
-        operators=("1.0 * x1 * x1",), correlators=("x1",), operatorRuns=op_runs,
+        enableBins=extra.pop("enableBins", False), nbrOfWalkersPerWorkGroup=1, enableParallelizePath=True,
+        enableGlobalPath=False, enableGlobalOldPath=False, enableRanlux=ranlux, luxuaryFactor=2,
+        ranluxIntMax=2 ** 32 - 1, operators=("1.0 * x1 * x1",), correlators=("x1",), operatorRuns=op_runs,
         metroStepsPerOperatorRun=msteps, seed=7, **extra)
     k = kernel.PIMCKernel(ka)
     if ranlux:
@@ -59,6 +59,31 @@ def test_ho_matches_exact_discretised_values(ranlux):
     mean, stderr = k.getCorrelator()
     # correlator: the sums over 20 runs of 2048 walkers; per-walker spread / sqrt(walkers)
     assert np.all(np.abs(mean[0, :8] - c[:8]) < 6 * stderr[0, :8] / np.sqrt(20) + 2e-3), (mean[0, :8], c[:8])
+    k.close()
+
+
+def test_ho_bins_follow_the_exact_gaussian():
+    """Known answer |psi_0|^2 (the reference tutorial's density plot): the discretised HO's
+    path marginal is exactly Gaussian with variance <x^2> = mean(1/lambda_k), so the bin
+    density (kernel.c:478-507, kernel.py:619-637) must follow N(0, <x^2>) averaged over each
+    bin; at beta = 8 that is the ground state's exp(-x^2)/sqrt(pi) to 0.1%."""
+    import math
+    require_gpu()
+    N, beta, lo, hi, nb = 64, 8.0, -3.0, 3.0, 30
+    k = _ho_kernel(N=N, beta=beta, enableBins=True, xMin=lo, xMax=hi, binResolutionPerDOF=nb)
+    for _ in range(5):
+        k.run()
+    k.zeroAccumulators()
+    for _ in range(10):
+        k.run()
+    d = k.getBinCounts()
+    assert d.shape == (nb,)
+    x2, _ = exact_ho(beta, N, [])
+    edges = np.linspace(lo, hi, nb + 1)
+    cdf = np.array([0.5 * (1.0 + math.erf(e / math.sqrt(2.0 * x2))) for e in edges])
+    want = np.diff(cdf) / np.diff(edges)
+    assert np.all(np.abs(d - want) < 5e-3 + 0.02 * want), np.abs(d - want).max()
+    assert abs(d.sum() * (hi - lo) / nb - (cdf[-1] - cdf[0])) < 2e-3
     k.close()
 
 
