@@ -39,10 +39,11 @@ def _pair(ranlux, walker_mode=False, compat=False):
     return ks, p0
 
 
-@pytest.mark.parametrize("chunks", [1, 3, 4, 64])
-@pytest.mark.parametrize("ranlux", [False, True], ids=["xorshift", "ranlux"])
-def test_run_host_equals_set_run_get(ranlux, chunks):
-    (a, b), p0 = _pair(ranlux)
+@pytest.mark.parametrize("chunks", [0, 1, 3, 4, 64])
+@pytest.mark.parametrize("ranlux,compat", [(False, False), (True, False), (False, True)],
+                         ids=["xorshift", "ranlux", "xorshift_compat"])
+def test_run_host_equals_set_run_get(ranlux, compat, chunks):
+    (a, b), p0 = _pair(ranlux, compat=compat)
     a.setPaths(p0)
     for _ in range(2):
         a.run(launches=2)
