@@ -212,14 +212,25 @@ def _set_cluster_code(obj, n: int, J: np.ndarray, reference_derivative: bool,
         terms = [f"{float(c)!r} * {xs[3 * k + dim]}" for k, c in enumerate(coefs) if abs(c) > 1e-15]
         return " + ".join(terms) if terms else "0.0"
 
-    # positions relative to the centre of mass, then pair sums
+    # pair vectors: straight from the Jacobi coordinates where that takes fewer terms (2-4
+    # atoms: the first pair is one Jacobi vector), else positions relative to the centre of
+    # mass and their differences
+    nnz = lambda v: int(np.sum(np.abs(v) > 1e-15))
+    direct = sum(nnz(BA[a] - BA[b]) for (a, b) in obj.pairs)
+    via_positions = sum(nnz(BA[a]) for a in range(n)) + len(obj.pairs)
     pos = []
-    for a in range(n):
-        for dim in range(3):
-            pos.append(f"    FLOAT_TYPE p{a}_{dim} = {comp(BA[a], dim)};")
     r2 = {}
-    for (a, b) in obj.pairs:
-        r2[(a, b)] = " + ".join(f"fs_sq(p{a}_{dim} - p{b}_{dim})" for dim in range(3))
+    if direct < via_positions:
+        for (a, b) in obj.pairs:
+            for dim in range(3):
+                pos.append(f"    FLOAT_TYPE d{a}_{b}_{dim} = {comp(BA[a] - BA[b], dim)};")
+            r2[(a, b)] = " + ".join(f"fs_sq(d{a}_{b}_{dim})" for dim in range(3))
+    else:
+        for a in range(n):
+            for dim in range(3):
+                pos.append(f"    FLOAT_TYPE p{a}_{dim} = {comp(BA[a], dim)};")
+        for (a, b) in obj.pairs:
+            r2[(a, b)] = " + ".join(f"fs_sq(p{a}_{dim} - p{b}_{dim})" for dim in range(3))
     body_pos = "\n".join(pos)
     pot_sum = " + ".join(f"lm2m2_r2({r2[p]})" for p in obj.pairs)
     vir_terms = []
