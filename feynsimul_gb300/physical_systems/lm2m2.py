@@ -113,10 +113,16 @@ inline FLOAT_TYPE dlm2m2_dr2(FLOAT_TYPE r2)
 
 
 def _lm2m2_c_code_branchless(reference_derivative: bool) -> str:
+    # Constants are folded where that saves operations: eps into every coefficient of V, and
+    # log2(e) into the exponents (exp(z) = exp2(z log2 e), the form the hardware evaluates):
+    # exp(x (beta x - alpha)) = exp2(x (beta' x - alpha')), and the damping
+    # exp(-(D/x - 1)^2) = exp2(-q^2) with q = max(D/x - 1, 0) sqrt(log2 e).
+    L = float(1.0 / np.log(2.0))
+    sL = float(np.sqrt(L))
     rm2 = RM * RM
     dr = D_CUT * RM
     tiny = 0.0005
-    B = 2.0 * np.pi / (X2_ADD - X1_ADD)
+    B = float(2.0 * np.pi / (X2_ADD - X1_ADD))
     # reference form of the add-on derivative term: Aa (cos(...) B + 1) = Aa (B sin(w) + 1)
     add_d = f"({A_ADD!r} * ({B!r} * sw + 1.0))" if reference_derivative else f"({A_ADD * B!r} * sw)"
     return f"""
@@ -126,12 +132,12 @@ inline FLOAT_TYPE lm2m2_r2(FLOAT_TYPE r2)
     FLOAT_TYPE ir = rsqrt(r2);
     FLOAT_TYPE x = r2 * ir * {1.0 / RM!r};
     FLOAT_TYPE ix2 = {rm2!r} * (ir * ir);
-    FLOAT_TYPE rat = ((({C10!r} * ix2 + {C8!r}) * ix2) + {C6!r}) * ix2 * ix2 * ix2;
-    FLOAT_TYPE q = fmax({dr!r} * ir - 1.0, 0.0);
-    rat = (r2 > {tiny * tiny!r}) ? rat * exp(-q * q) : 0.0;
+    FLOAT_TYPE rat = ((({EPS_K * C10!r} * ix2 + {EPS_K * C8!r}) * ix2) + {EPS_K * C6!r}) * ix2 * ix2 * ix2;
+    FLOAT_TYPE q = fmax({dr * sL!r} * ir - {sL!r}, 0.0);
+    rat = (r2 > {tiny * tiny!r}) ? rat * exp2(-q * q) : 0.0;
     FLOAT_TYPE w = {B!r} * (x - {X1_ADD!r});
-    FLOAT_TYPE add = (x >= {X1_ADD!r} && x <= {X2_ADD!r}) ? {A_ADD!r} : 0.0;
-    return {EPS_K!r} * ({A_STAR!r} * exp(x * ({BETA_STAR!r} * x - {ALPHA!r})) - rat + add * (1.0 - cos(w)));
+    FLOAT_TYPE add = (x >= {X1_ADD!r} && x <= {X2_ADD!r}) ? {EPS_K * A_ADD!r} : 0.0;
+    return {EPS_K * A_STAR!r} * exp2(x * ({L * BETA_STAR!r} * x - {L * ALPHA!r})) - rat + add * (1.0 - cos(w));
 }}
 inline FLOAT_TYPE dlm2m2_dr2(FLOAT_TYPE r2)
 {{
@@ -147,9 +153,9 @@ inline FLOAT_TYPE dlm2m2_dr2(FLOAT_TYPE r2)
     FLOAT_TYPE dfr = (r2 > {tiny * tiny!r}) ? F * drat + F * (2.0 * q * {D_CUT!r} * ix2) * rat : 0.0;
     FLOAT_TYPE sw = sin({B!r} * (x - {X1_ADD!r}));
     FLOAT_TYPE inwin = (x >= {X1_ADD!r} && x <= {X2_ADD!r}) ? 1.0 : 0.0;
-    FLOAT_TYPE dv = {A_STAR!r} * exp(x * ({BETA_STAR!r} * x - {ALPHA!r})) * ({2.0 * BETA_STAR!r} * x - {ALPHA!r})
+    FLOAT_TYPE dv = {A_STAR!r} * exp2(x * ({L * BETA_STAR!r} * x - {L * ALPHA!r})) * ({2.0 * BETA_STAR!r} * x - {ALPHA!r})
                     - dfr + inwin * {add_d};
-    return {EPS_K!r} * dv * ir * {0.5 / RM!r};
+    return dv * ir * {EPS_K * 0.5 / RM!r};
 }}
 """
 
