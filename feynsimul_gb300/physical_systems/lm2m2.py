@@ -113,10 +113,11 @@ inline FLOAT_TYPE dlm2m2_dr2(FLOAT_TYPE r2)
 
 
 def _lm2m2_c_code_branchless(reference_derivative: bool) -> str:
-    # Constants are folded where that saves operations: eps into every coefficient of V, and
-    # log2(e) into the exponents (exp(z) = exp2(z log2 e), the form the hardware evaluates):
-    # exp(x (beta x - alpha)) = exp2(x (beta' x - alpha')), and the damping
-    # exp(-(D/x - 1)^2) = exp2(-q^2) with q = max(D/x - 1, 0) sqrt(log2 e).
+    # Constants are folded where that saves operations: eps and the powers of r_m into every
+    # coefficient of V, so it is written in r rather than x = r / r_m, and log2(e) into the
+    # exponents (exp(z) = exp2(z log2 e), the form the hardware evaluates):
+    # exp(x (beta x - alpha)) = exp2(r (beta' r - alpha')), and the damping
+    # exp(-(D/x - 1)^2) = exp2(-q^2) with q = max(D r_m / r - 1, 0) sqrt(log2 e).
     L = float(1.0 / np.log(2.0))
     sL = float(np.sqrt(L))
     rm2 = RM * RM
@@ -130,14 +131,14 @@ inline FLOAT_TYPE fs_sq(FLOAT_TYPE v) {{ return v * v; }}
 inline FLOAT_TYPE lm2m2_r2(FLOAT_TYPE r2)
 {{
     FLOAT_TYPE ir = rsqrt(r2);
-    FLOAT_TYPE x = r2 * ir * {1.0 / RM!r};
-    FLOAT_TYPE ix2 = {rm2!r} * (ir * ir);
-    FLOAT_TYPE rat = ((({EPS_K * C10!r} * ix2 + {EPS_K * C8!r}) * ix2) + {EPS_K * C6!r}) * ix2 * ix2 * ix2;
+    FLOAT_TYPE r = r2 * ir;
+    FLOAT_TYPE u = ir * ir;
+    FLOAT_TYPE rat = ((({EPS_K * C10 * RM ** 10!r} * u + {EPS_K * C8 * RM ** 8!r}) * u) + {EPS_K * C6 * RM ** 6!r}) * u * u * u;
     FLOAT_TYPE q = fmax({dr * sL!r} * ir - {sL!r}, 0.0);
     rat = (r2 > {tiny * tiny!r}) ? rat * exp2(-q * q) : 0.0;
-    FLOAT_TYPE w = {B!r} * (x - {X1_ADD!r});
-    FLOAT_TYPE add = (x >= {X1_ADD!r} && x <= {X2_ADD!r}) ? {EPS_K * A_ADD!r} : 0.0;
-    return {EPS_K * A_STAR!r} * exp2(x * ({L * BETA_STAR!r} * x - {L * ALPHA!r})) - rat + add * (1.0 - cos(w));
+    FLOAT_TYPE w = {B / RM!r} * r - {B * X1_ADD!r};
+    FLOAT_TYPE add = (r >= {X1_ADD * RM!r} && r <= {X2_ADD * RM!r}) ? {EPS_K * A_ADD!r} : 0.0;
+    return {EPS_K * A_STAR!r} * exp2(r * ({L * BETA_STAR / RM ** 2!r} * r - {L * ALPHA / RM!r})) - rat + add * (1.0 - cos(w));
 }}
 inline FLOAT_TYPE dlm2m2_dr2(FLOAT_TYPE r2)
 {{
