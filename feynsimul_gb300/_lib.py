@@ -20,6 +20,7 @@ FS_ERR_TIMEOUT = -5
 FS_ERR_IO = -6
 FS_ERR_CUDA = -7
 FS_ERR_STATE = -8
+FS_ERR_NUMERIC = -9
 
 ACCUM_REF_FP32, ACCUM_FP64, ACCUM_KAHAN, ACCUM_STUDY = 0, 1, 2, 3
 

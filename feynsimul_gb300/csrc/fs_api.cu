@@ -95,7 +95,8 @@ struct fs_handle {
     uint32_t *d_rtab = nullptr, *d_gtab = nullptr, *d_bins = nullptr;
     void *d_ops = nullptr, *d_cor = nullptr;
     unsigned long long *d_hist = nullptr;
-    int *d_status = nullptr;
+    int *d_status = nullptr;   // [0] FS_STATUS_* flags, [1] 1 + a walker that raised one
+    bool status_pending = false;  // a sweep ran since fs_sync last read d_status
     void *d_mlp_frag = nullptr;
     float *d_mlp_bias = nullptr;
     double mlp_inv_scale = 1.0;
@@ -1064,6 +1065,7 @@ extern "C" int fs_run(fs_handle *h, int32_t n_launches)
     }
     CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), FS_ERR_CUDA);
     h->timed = true;
+    h->status_pending = true;
     return FS_OK;
 }
 
@@ -1119,6 +1121,7 @@ extern "C" int fs_run_host(fs_handle *h, const void *paths_in, void *paths_out, 
         h->steps_done += per_launch * (unsigned long long)n_launches;
         CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), FS_ERR_CUDA);
         h->timed = true;
+        h->status_pending = true;
         return FS_OK;
     }
     if (!h->s_in) CUDA_TRY(h, cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking), FS_ERR_CUDA);
@@ -1173,6 +1176,7 @@ extern "C" int fs_run_host(fs_handle *h, const void *paths_in, void *paths_out, 
     CUDA_TRY(h, cudaStreamWaitEvent(h->stream, e_c2, 0), FS_ERR_CUDA);
     CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream), FS_ERR_CUDA);
     h->timed = true;
+    h->status_pending = true;
     return FS_OK;
 }
 
@@ -1227,12 +1231,29 @@ static void fill_args(fs_handle *h, FsArgsHost &a)
     a.block_offset = 0;
 }
 
+// After the stream has drained: the status word the sweeps since the last check wrote
+// (fs_pimc.cuh, FS_STATUS_*), cleared once read.
+static int check_status(fs_handle *h)
+{
+    if (!h->status_pending) return FS_OK;
+    int st[2] = {0, 0};
+    CUDA_TRY(h, cudaMemcpyAsync(st, h->d_status, sizeof st, cudaMemcpyDeviceToHost, h->stream), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
+    h->status_pending = false;
+    if (!st[0]) return FS_OK;
+    CUDA_TRY(h, cudaMemsetAsync(h->d_status, 0, sizeof st, h->stream), FS_ERR_CUDA);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
+    return fail(h, FS_ERR_NUMERIC,
+                "walker %d: a path value is not finite (NaN or infinity) after the sweep; the paths and the "
+                "operator, correlator and histogram sums of this run are not usable", st[1] - 1);
+}
+
 extern "C" int fs_sync(fs_handle *h)
 {
     if (!h) return FS_ERR_CONFIG;
     CUDA_TRY(h, cudaSetDevice(h->device), FS_ERR_CUDA);
     CUDA_TRY(h, cudaStreamSynchronize(h->stream), FS_ERR_LAUNCH);
-    return FS_OK;
+    return check_status(h);
 }
 
 // host watchdog: poll the stream instead of blocking forever (kernel.py:499-506 analogue)
@@ -1243,7 +1264,7 @@ extern "C" int fs_sync_timeout(fs_handle *h, double seconds)
     auto t0 = std::chrono::steady_clock::now();
     for (;;) {
         cudaError_t e = cudaStreamQuery(h->stream);
-        if (e == cudaSuccess) return FS_OK;
+        if (e == cudaSuccess) return check_status(h);
         if (e != cudaErrorNotReady) return fail(h, FS_ERR_LAUNCH, "stream error: %s", cudaGetErrorString(e));
         double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (el > seconds)

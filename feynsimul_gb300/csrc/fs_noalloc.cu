@@ -13,7 +13,10 @@
 // no ordering between them) race on it, and the later copy can overwrite seeds the earlier
 // kernel is still reading.  The kernel reads only the rows the same call copied in, so
 // nothing in the array needs to start at zero, and whatever the previous call left there
-// is never read.
+// is never read.  The array's device address is looked up once per device and kept for
+// the life of the process; a device reset (cudaDeviceReset, or a primary-context reset by
+// another library) frees the image that holds the array, so the kept address is stale
+// after one and the entry point must not be called again in that process.
 #include <cuda_runtime.h>
 
 #include <mutex>

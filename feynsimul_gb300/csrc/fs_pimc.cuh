@@ -396,7 +396,7 @@ struct FsArgs {
     void *cor_means;           // [walkers][nCorr][N/2]
     fs_u32 *bins;              // [res^DOF]
     fs_u64 *hist;              // [hist bins]
-    int *status;
+    int *status;               // [0] flags (FS_STATUS_*), [1] 1 + a walker that raised one
     double opnorm;
     FT *shift_old;             // path shift, fixed mode: the shifted row before the move [walkers][N]
     unsigned long long step_base;  // fixed mode: Metropolis steps of earlier launches
@@ -469,6 +469,17 @@ __device__ __forceinline__ void fs_kahan(float &s, float &c, float x)
     const float t = __fadd_rn(s, y);
     c = __fsub_rn(__fsub_rn(t, s), y);
     s = t;
+}
+
+// Status word: a path value that is not finite (NaN or infinity) at the end of a launch.
+// Every path value passes through the launch's path-out copy (or, for global paths, the
+// owner's final check), so one compare per value per launch finds any walker whose
+// proposals or potential blew up; the host reads the word at fs_sync.
+#define FS_STATUS_NONFINITE 1
+__device__ __forceinline__ void fs_flag_nonfinite(int *status, int walker)
+{
+    atomicOr(status, FS_STATUS_NONFINITE);
+    atomicCAS(status + 1, 0, walker + 1);
 }
 
 #ifndef FS_RNG_ONLY
@@ -947,6 +958,23 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                 if (tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = cacc[c][j];
             }
 #endif
+#if FS_GLOBAL
+        {
+            // the walker's slices this thread owns, checked in place (the shared-memory
+            // mode checks every value in its path-out copy instead)
+#if FS_PARALLEL
+            const int c_lo = t * FS_SEG, c_hi = (t + 1) * FS_SEG;
+#else
+            const int c_lo = 0, c_hi = FS_N;
+#endif
+            bool bad = false;
+#pragma unroll 1
+            for (int s = c_lo; s < c_hi; s++)
+#pragma unroll
+                for (int d = 0; d < FS_DOF; d++) bad |= !isfinite(FS_AT(P, d, s));
+            if (bad) fs_flag_nonfinite(a.status, w);
+        }
+#endif
 #if FS_RANLUX
         fs_rl_store(fs.st, a.rtab + (size_t)tid * 28);
         FS_WSYNC();
@@ -973,7 +1001,9 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         for (int i = tid_b; i < count; i += FS_BLOCK) {
             const int wi = i / (FS_DOF * FS_N), r = i - wi * (FS_DOF * FS_N);
             const int d = r / FS_N, sl = r - d * FS_N;
-            a.paths[base + i] = FS_AT(s_path + wi * FS_WSTRIDE, d, sl);
+            const FT v = FS_AT(s_path + wi * FS_WSTRIDE, d, sl);
+            a.paths[base + i] = v;
+            if (!isfinite(v)) fs_flag_nonfinite(a.status, w0 + wi);
         }
 #endif
 #if FS_NHIST > 0

@@ -434,7 +434,12 @@ class PIMCKernel:
         The device keeps running sums.  The reference divides by one run's count however many
         runs were made (its buffer is never re-zeroed); reference-compatible mode repeats
         that, otherwise the sums are divided by the runs made since creation or
-        zeroAccumulators()."""
+        zeroAccumulators().
+
+        The standard error is that of the mean: the per-walker spread / sqrt(walkers) of the
+        same normalised values.  The reference leaves its standard error in raw-sum units,
+        operatorRuns * N times the mean's scale (kernel.py:613-616); reference-compatible
+        mode repeats that."""
         if not self._enableCorrelator:
             raise Exception("Can only return correlator when created with"
                             "kernalArg.enableCorrelator = True")
@@ -444,9 +449,29 @@ class PIMCKernel:
         vals = raw.reshape(self._nbrOfWalkers, len(self._correlators), self._N // 2)
         runs = 1 if self._compat else max(1, self._runsSinceZero)
         vals = vals / float(runs)
-        mean = vals.mean(axis=0) / float(self._operatorRuns * self._N)
+        scale = float(self._operatorRuns * self._N)
+        mean = vals.mean(axis=0) / scale
         se = vals.std(axis=0) / np.sqrt(self._nbrOfWalkers)
+        if not self._compat:
+            se = se / scale
         return (mean, se)
+
+    def getCorrelatorPerWalker(self):
+        """Each walker's correlator mean, shape (walkers, nCorr, N/2), with getCorrelator's
+        normalisation (its mean over the walkers is getCorrelator's mean); the FP64 column
+        in "study" accumulation.  Used to merge replicas and for batch errors."""
+        if not self._enableCorrelator:
+            raise Exception("Can only return correlator when created with"
+                            "kernalArg.enableCorrelator = True")
+        raw = self._raw_correlator()
+        if self._accumulation == "study":
+            raw = raw.reshape(-1, 4)[:, 3]
+        return raw.reshape(self._nbrOfWalkers, len(self._correlators), self._N // 2) * self._cor_norm()
+
+    def getMovesPerRun(self):
+        """Moves each work-item makes in one run: the steps times the move types per step
+        (the denominator of the per-move acceptance rate)."""
+        return self._operatorRuns * self._metroStepsPerOperatorRun * self._movesPerStep
 
     def _cor_count(self):
         return self._nbrOfWalkers * len(self._correlators) * (self._N // 2) * \

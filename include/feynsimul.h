@@ -51,6 +51,7 @@ extern "C" {
 #define FS_ERR_IO (-6)       /* host buffer size mismatch */
 #define FS_ERR_CUDA (-7)     /* any other CUDA runtime error */
 #define FS_ERR_STATE (-8)    /* call not valid for this handle's configuration */
+#define FS_ERR_NUMERIC (-9)  /* a sweep left a non-finite path value (fs_sync / fs_sync_timeout) */
 
 /* accumulation of operator / correlator running sums */
 #define FS_ACCUM_REF_FP32 0  /* FP32 sums in the reference's order (kernel.c:622, :784) */
@@ -194,7 +195,14 @@ int fs_get_last_chunks(const fs_handle *h, int32_t *chunks);
 /* page-lock / release a host buffer (cudaHostRegister) for overlapped copies */
 int fs_pin_host(void *ptr, size_t bytes);
 int fs_unpin_host(void *ptr);
+/* Wait for the handle's queued work (kernel.py:500).  Then read the sweeps' status word:
+ * if a launch since the last check left a path value that is not finite (NaN or infinity:
+ * a potential or operator that diverged), return FS_ERR_NUMERIC naming one such walker
+ * (fs_last_error) and clear the word.  No counterpart in the reference, which does not
+ * look at its paths. */
 int fs_sync(fs_handle *h);
+/* fs_sync that gives up after `seconds` with FS_ERR_TIMEOUT, polling the stream (the
+ * reference's failure path is its wait on the kernel event, kernel.py:499-506) */
 int fs_sync_timeout(fs_handle *h, double seconds);
 
 /* Raw device results.  Operators: [n_threads][n_ops] per-thread means (FP32 values for
@@ -261,7 +269,10 @@ int fs_rng_xorshift_stream(uint32_t *states, int32_t n_streams, int32_t n_draws,
  * default stream): synchronise before reading the table.  xs may be reused when the call
  * returns only if it is pageable host memory.  Calls share the scratch array, so calls
  * that can overlap on the GPU race.  The first call on a device looks up the array's
- * device address; make that first call before any stream capture. */
+ * device address and keeps it for the life of the process; make that first call before any
+ * stream capture.  A device reset (cudaDeviceReset, or another library resetting the
+ * primary context) invalidates the kept address: do not call this entry point again in a
+ * process after such a reset. */
 int fs_ranlux_init_noalloc(uint32_t *table, const uint64_t *xs, size_t n_rows, void *stream);
 
 /* ---- learned bisection proposal (no counterpart in the reference) ----

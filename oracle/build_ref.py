@@ -2,7 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``tests/golden/make_golden.py`` and the
 oracle may use this module; the product never does.  It needs the reference's source tree
-(``REFERENCE_ROOT``); everything it builds goes to ``oracle/_ref/`` (git-ignored).  Where
+(``REFERENCE_ROOT``: the ``FEYNSIMUL_REFERENCE_ROOT`` environment variable, else the
+development container's mount); everything it builds goes to ``oracle/_ref/`` (git-ignored).  Where
 the tree is absent nothing here runs: the goldens it produces are committed under
 ``tests/golden/``.
 
@@ -34,7 +35,9 @@ import types
 
 import numpy as np
 
-REFERENCE_ROOT = "/root/reference"
+# The reference's source tree: the FEYNSIMUL_REFERENCE_ROOT environment variable, else the
+# read-only mount this recipe was written for.
+REFERENCE_ROOT = os.environ.get("FEYNSIMUL_REFERENCE_ROOT") or "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BUILD = os.path.join(HERE, "_ref")
 
