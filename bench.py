@@ -84,6 +84,25 @@ def workload_overrides(args):
     return o
 
 
+def bench_config(workload, ka):
+    """The workload keys of the JSON line, identical in both arms (the reference arm times a
+    bounded sample of the same workload; its sample is described in its cpu_baseline)."""
+    return {"workload": workload, "sweeps_per_step": ka["operatorRuns"] * ka["metroStepsPerOperatorRun"],
+            "node_updates_per_step": node_updates_per_run(ka)}
+
+
+def _json_safe(obj):
+    if isinstance(obj, dict):
+        return {k: _json_safe(v) for k, v in obj.items()}
+    if isinstance(obj, (list, tuple)):
+        return [_json_safe(v) for v in obj]
+    if isinstance(obj, np.ndarray):
+        return obj.tolist()
+    if isinstance(obj, np.generic):
+        return obj.item()
+    return obj
+
+
 def node_updates_per_run(ka):
     seg = 2 ** ka["S"]
     tpw = ka["N"] // seg
@@ -219,24 +238,6 @@ def oracle_cpu_rate(sysm, ka, extra, seconds=10.0, walkers=None):
                       f"sweep(s) ({nodes} node updates, {dt:.1f} s), oracle C restatement, OpenMP over walkers"}
 
 
-def integrated_autocorr(series):
-    """Sokal automatic windowing (c = 5) of the normalised autocorrelation; series[t, walker]."""
-    x = series - series.mean(axis=0, keepdims=True)
-    n = x.shape[0]
-    if n < 4:
-        return 0.5
-    var = (x * x).mean()
-    if var <= 0:
-        return 0.5
-    tau = 0.5
-    for t in range(1, n // 2):
-        rho = (x[:-t] * x[t:]).mean() / var
-        tau += rho
-        if t >= 5 * tau:
-            break
-    return max(tau, 0.5)
-
-
 # register budget the sweep kernel is compiled for, per workload (launch-shape sweep on GB300)
 TUNED_MIN_BLOCKS = {"he3": 7, "ho": 0}
 TUNED_WPB = {"he3": 4, "ho": 0}
@@ -307,9 +308,11 @@ def roofline_for(config, ka, node_rate, clk, default_workload=True):
 # ------------------------------------------------------------------ learned vs plain
 def learned_study(quick=True):
     """Energy-estimator ESS/s of the plain sampler and of the learned level-1 proposal on the
-    He3 workload (feynsimul_gb300.learned.ess_study).  ESS from Sokal-windowed integrated
-    autocorrelation of per-walker energies measured after every launch of 4 sweeps, all
-    samplers from the same equilibrated paths; training time is not included in ESS/s."""
+    He3 workload (feynsimul_gb300.learned.ess_study), by the package's one definition
+    (learned.energy_ess): per-walker energies measured after every sweep, 200 measurements
+    per walker, Sokal-windowed integrated autocorrelation, ESS over the wall time of the
+    measured loop; all samplers from the same equilibrated paths; training time is not
+    included in ESS/s."""
     from feynsimul_gb300 import build as fb
     fb.build()
     from feynsimul_gb300.learned import ess_study
@@ -318,15 +321,15 @@ def learned_study(quick=True):
     t0 = time.perf_counter()
     res = ess_study(sysm, sysm.beta, 256, 16384,
                     S_plain=(4, 5) if quick else (3, 4, 5, 6), S_learned=(4, 5) if quick else (4, 5, 6, 7),
-                    launches=40 if quick else 60, train_steps=1500 if quick else 3000,
+                    launches=200, train_steps=1500 if quick else 3000,
                     kernel_extra=dict(enableRanlux=True, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
                                       walkersPerBlock=TUNED_WPB["he3"], minBlocksPerSM=TUNED_MIN_BLOCKS["he3"]),
                     log=lambda *a: None)
     out = {"metric": "energy ESS/s, learned vs plain sampler (He3 LM2M2 T=1K N=256 16384 walkers RANLUX)",
            "summary": res["summary"], "wall_s": time.perf_counter() - t0,
-           "plain": {str(k): {kk: v[kk] for kk in ("acceptance", "tau_int_launches", "ess_per_s",
+           "plain": {str(k): {kk: v[kk] for kk in ("acceptance", "tau_int_sweeps", "ess_per_s",
                                                     "node_updates_per_s")} for k, v in res["plain"].items()},
-           "learned": {str(k): {kk: v[kk] for kk in ("acceptance", "tau_int_launches", "ess_per_s",
+           "learned": {str(k): {kk: v[kk] for kk in ("acceptance", "tau_int_sweeps", "ess_per_s",
                                                       "node_updates_per_s", "loss_start", "loss_end",
                                                       "validation_gain_nats", "fallback")}
                        for k, v in res["learned"].items()}}
@@ -515,6 +518,8 @@ def precision_bench(args):
         kw["op_runs"] = args.op_runs
     if args.msteps:
         kw["msteps"] = args.msteps
+    if args.minb > 0:
+        kw["min_blocks"] = args.minb
     import torch
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()        # sampled over the whole study: both arms' timed launches are inside
@@ -533,6 +538,55 @@ def precision_bench(args):
             "value": r["fp32_node_updates_per_s"], "unit": "node-updates/s (FP32 path, study sums)",
             "n_gpus": 1, "higher_is_better": True, "dtype": "f32 path, f64/f32/kahan sums",
             "data": "synthetic, seeded", "config": {"workload": r["workload"]}, "study": r}
+
+
+def _compact_merge(m):
+    """The replica merge of every accumulator, shortened for the JSON line: histogram and
+    bin counts as totals."""
+    out = {k: v for k, v in m.items() if k not in ("histogram_counts", "bin_counts")}
+    if "histogram_counts" in m:
+        out["histogram_total_counts"] = int(np.sum(m["histogram_counts"]))
+    if "bin_counts" in m:
+        out["bin_total_counts"] = int(np.sum(m["bin_counts"]))
+    return out
+
+
+def oracle_cpu_ess(sysm, ka, extra, paths, launches=200, burn=10, walkers=64):
+    """The CPU baseline of the energy ESS/s: the oracle's C restatement on the host cores with
+    the same definition as learned.energy_ess (one measurement per walker after every sweep,
+    Sokal window, ESS over the wall time of the measured loop incl. the per-walker energy
+    reduction), on `walkers` walkers started from the given equilibrated paths."""
+    from oracle import oracle as orc
+    from feynsimul_gb300.stats import ess
+    cores = cpu_cores()
+    W = min(walkers, ka["nbrOfWalkers"])
+    cfg = orc.OracleConfig(
+        DOF=sysm.DOF, potential=sysm.potential, userCode=sysm.userCode, nbrOfWalkers=W, N=ka["N"],
+        beta=ka["beta"], S=ka["S"], operatorRuns=1, metroStepsPerOperatorRun=1, nbrOfWalkersPerWorkGroup=1,
+        enableParallelizePath=True, enableRanlux=ka["enableRanlux"], luxuaryFactor=ka.get("luxuaryFactor", 2),
+        ranluxIntMax=ka.get("ranluxIntMax", 2 ** 32 - 1), operators=ka["operators"], compat=False, accum=1)
+    o = orc.OracleSampler(cfg, omp_threads=cores)
+    o.paths[...] = paths[:W]
+    if ka["enableRanlux"]:
+        o.init_ranlux_rows(o.ranlux_tab, (np.uint64(777) << np.uint64(32)) + np.arange(o.ranlux_tab.shape[0], dtype=np.uint64))
+        o.init_ranlux_rows(o.group_tab, (np.uint64(778) << np.uint64(32)) + np.arange(o.group_tab.shape[0], dtype=np.uint64))
+    else:
+        rs = np.random.RandomState(3)
+        o.seeds[...] = rs.randint(0, 2 ** 31 - 1, size=o.seeds.shape)
+        o.walker_seeds[...] = rs.randint(0, 2 ** 31 - 1, size=o.walker_seeds.shape)
+    T = ka["N"] // 2 ** ka["S"]
+    for _ in range(burn):
+        o.run()
+    series = []
+    t0 = time.perf_counter()
+    for _ in range(launches):
+        o.run()
+        series.append(o.op_means.reshape(W, T, -1)[:, :, 0].mean(axis=1))
+    wall = time.perf_counter() - t0
+    e, tau = ess(np.array(series))
+    return {"value": e / wall, "unit": "effective energy samples/s", "cores": cores, "kind": "port",
+            "tau_int_sweeps": float(tau), "sample": f"{W} walkers x {launches} sweeps, one measurement per sweep "
+            f"({wall:.1f} s), oracle C restatement, OpenMP over walkers"}
 
 
 def run_gb300(args, rank, world):
@@ -612,11 +666,27 @@ def run_gb300(args, rank, world):
     h2d = host_paths.nbytes
     d2h = ops.nbytes + host_paths.nbytes   # per-walker operator means + the paths
 
-    # energy ESS/s from the per-run per-walker energy series of the e2e loop
     series = np.array(energies)  # [steps, walkers]
-    tau = integrated_autocorr(series)
-    ess = series.shape[0] * series.shape[1] / (2.0 * tau)
-    ess_per_s = ess / (ms_per_step * 1e-3 * args.steps)
+
+    # ---- energy ESS/s (learned.energy_ess): one measurement per walker after every sweep,
+    # 200 measurements, ESS over the wall time of that loop, from the equilibrated paths ----
+    ess_rec = None
+    if args.config == "he3" and not args.no_ess:
+        from feynsimul_gb300.learned import energy_ess
+        ka_e = dict(ka, operatorRuns=1, metroStepsPerOperatorRun=1)
+        ke = PIMCKernel(KernelArgs(system=sysm, seed=replica_seed(2000, rank), walkersPerBlock=wpb,
+                                   minBlocksPerSM=minb, **extra, **ka_e))
+        ke.setPaths(host_paths)
+        if ka["enableRanlux"]:
+            ke.initRanlux()
+            ke.groupInitRanlux()
+        m = energy_ess(ke, launches=args.ess_launches, burn=10)
+        ser = m.pop("series")
+        ke.close()
+        ess_rec = dict(m, ess=group.sum(m["ess"]), ess_per_s=group.sum(m["ess"]) / group.max(m["wall_s"]),
+                       unit="effective energy samples/s", energy_mean=float(ser.mean()),
+                       definition="learned.energy_ess: per-walker virial energy after every sweep, Sokal "
+                                  "window (c=5), ESS / wall time of the measured loop incl. reads")
 
     # ---- roofline: the sweep is bound by instruction issue (see roofline_for) ----
     roof = roofline_for(args.config, ka, value / world, clk,
@@ -628,22 +698,23 @@ def run_gb300(args, rank, world):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (u32 RNG, f64 sums)",
         "data": "synthetic, seeded",
-        "config": {"workload": workload, "sweeps_per_step": ka["operatorRuns"] * ka["metroStepsPerOperatorRun"],
-                   "node_updates_per_step": nodes, "l2": "flushed between launches (512 MiB write)",
-                   "parallelism": f"replicas x{world}", "walkers_per_block": int(info.walkers_per_block),
-                   "registers": int(info.registers), "smem_bytes": int(info.smem_bytes)},
+        "config": bench_config(workload, ka),
+        "timing": {"l2": "flushed between launches (512 MiB write)", "parallelism": f"replicas x{world}"},
+        "launch": {"walkers_per_block": int(info.walkers_per_block), "registers": int(info.registers),
+                   "smem_bytes": int(info.smem_bytes), "grid": int(info.grid_blocks)},
         "e2e": {"value": e2e_value, "unit": "node-updates/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "pinned": pinned, "api": "PIMCKernel.runHost + getOperators",
                 "chunks": k.lastChunks},
-        "energy_ess_per_s": ess_per_s, "energy_tau_int_runs": tau,
+        "energy_ess": ess_rec,
         "energy_mean": float(series[series.shape[0] // 2:].mean()),
         "energy_all_replicas": group.merge(series[series.shape[0] // 2:].mean(axis=0)),
+        "accumulators_all_replicas": _json_safe(_compact_merge(group.merge_kernel(k))),
         "acceptance_rate": float(k.getAcceptanceRate()),
         "gpu_launches": args.steps * (2 + k.lastChunks),  # sweeps, pipelined chunks, walker reductions
         "roofline": roof, "clocks": clk,
     }
     k.close()
-    return result, (sysm, ka, extra)
+    return result, (sysm, ka, extra, host_paths)
 
 
 def main():
@@ -664,6 +735,9 @@ def main():
     ap.add_argument("--chunks", type=int, default=0,
                     help="walker chunks pipelined in the e2e step (0 = automatic, 1 = no overlap)")
     ap.add_argument("--systems", type=int, default=64, help="batch config: number of systems (small profiling cases)")
+    ap.add_argument("--no-ess", action="store_true", help="skip the energy ESS/s measurement")
+    ap.add_argument("--ess-launches", type=int, default=200, help="measurements per walker of the ESS loop")
+    ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch sub-record of the default run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -686,7 +760,7 @@ def main():
         out = {"impl": "reference", "metric": "path-node updates/s (plain Metropolis-bisection sampler)",
                "value": v, "unit": "node-updates/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-               "data": "synthetic, seeded", "config": {"workload": workload},
+               "data": "synthetic, seeded", "config": bench_config(workload, ka),
                "cpu_baseline": dict(cb, value=v),
                "e2e": {"value": v, "unit": "node-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                "note": "the reference's OpenCL kernels need an OpenCL CPU platform, which is absent; this "
@@ -711,13 +785,24 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    result, (sysm, ka, extra) = run_gb300(args, rank, world)
+    result, (sysm, ka, extra, paths_eq) = run_gb300(args, rank, world)
     if rank == 0:
         if args.config == "he3" and not args.no_learned:
             result["learned_vs_plain"] = learned_study(quick=True)["summary"]
         if not args.no_cpu_baseline:
             result["cpu_baseline"] = oracle_cpu_rate(sysm, ka, extra, seconds=args.cpu_seconds)
-        print(json.dumps(result))
+            if result.get("energy_ess"):
+                result["energy_ess"]["cpu_baseline"] = oracle_cpu_ess(sysm, ka, extra, paths_eq,
+                                                                      launches=args.ess_launches)
+        if args.config == "he3" and not args.no_batch:
+            # the ragged batch (64 LM2M2 systems in one persistent launch) as a sub-record
+            bargs = argparse.Namespace(**vars(args))
+            bargs.steps, bargs.warmup, bargs.cpu_seconds = min(args.steps, 5), 3, min(args.cpu_seconds, 6.0)
+            br = batch_bench(bargs)
+            result["ragged_batch"] = {k: br[k] for k in ("metric", "value", "unit", "ms_per_step", "steps",
+                                                         "roofline", "clocks", "config", "gpu_launches",
+                                                         "cpu_baseline") if k in br}
+        print(json.dumps(_json_safe(result)))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -224,12 +224,13 @@ __device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream 
                     continue;
                 }
 #endif
-                FT rz = (FT)0;
-                if (v != (FT)0) {
-                    // sigma_n * sqrt(-2 log v) * sin(2 pi u), left to right (kernel.c:352-353)
-                    rz = FS_MUL(FS_MUL(sig, FS_SQRT(FS_MUL((FT)-2, FS_LOG(v)))),
-                                FS_SIN(FS_MUL((FT)FS_TWO_PI, u)));
-                }
+                // sigma_n * sqrt(-2 log v) * sin(2 pi u), left to right (kernel.c:352-353), or 0
+                // for v == 0 (kernel.c:349-351).  Evaluated unconditionally and selected: log 0
+                // is -inf, so that lane's product is infinite or NaN and is discarded, and no
+                // branch is taken per degree of freedom.
+                FT rz = FS_MUL(FS_MUL(sig, FS_SQRT(FS_MUL((FT)-2, FS_LOG(v)))),
+                               FS_SIN(FS_MUL((FT)FS_TWO_PI, u)));
+                rz = v != (FT)0 ? rz : (FT)0;
                 FS_AT(P, d, m) = FS_ADD(FS_MUL((FT)0.5, FS_ADD(FS_AT(P, d, l), FS_AT(P, d, r))), rz);
             }
         }

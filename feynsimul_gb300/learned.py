@@ -238,19 +238,43 @@ class LearnedProposal:
 
 # ------------------------------------------------------------------ ESS study
 def energy_series(kernel, launches, op_index=0):
-    """Per-walker operator means of `launches` consecutive runs and their device time."""
+    """Per-walker operator means of `launches` consecutive runs: (series[launch, walker],
+    device seconds of the sweeps, wall seconds of the whole loop including the per-run
+    reads of the operator means)."""
+    import time
     series, t = [], 0.0
+    t0 = time.perf_counter()
     for _ in range(launches):
         kernel.run()
         t += kernel.getRunTime()
         series.append(kernel.getOperators()[op_index])
-    return np.array(series), t
+    return np.array(series), t, time.perf_counter() - t0
 
 
-def ess_study(system, beta, N, walkers, S_plain=(3, 4, 5, 6), S_learned=(4, 5, 6, 7), launches=60,
-              op_runs=1, msteps=4, burn=10, train_steps=3000, harvest_snapshots=4, seed=1,
+def energy_ess(kernel, launches=200, burn=10):
+    """Energy-estimator effective samples per second, the one definition this package
+    reports: after ``burn`` runs, ``launches`` runs of the kernel (each run one operator
+    measurement per walker, i.e. operatorRuns = 1), the integrated autocorrelation time of
+    the per-walker energy series by Sokal's automatic window (stats.ess), and ESS divided by
+    the wall time of the measured loop (sweeps, measurements and the reads of the
+    per-walker energies)."""
+    from .stats import ess, tau_int_batch_means
+    for _ in range(burn):
+        kernel.run()
+    series, dev_s, wall_s = energy_series(kernel, launches)
+    e, tau = ess(series)
+    sweeps = kernel._operatorRuns * kernel._metroStepsPerOperatorRun
+    return {"ess": float(e), "ess_per_s": float(e / wall_s), "tau_int_measurements": float(tau),
+            "tau_int_sweeps": float(tau * sweeps), "tau_batch_means": float(tau_int_batch_means(series)),
+            "measurements_per_walker": int(launches), "sweeps_per_measurement": int(sweeps),
+            "wall_s": float(wall_s), "device_s": float(dev_s), "series": series}
+
+
+def ess_study(system, beta, N, walkers, S_plain=(3, 4, 5, 6), S_learned=(4, 5, 6, 7), launches=200,
+              op_runs=1, msteps=1, burn=10, train_steps=3000, harvest_snapshots=4, seed=1,
               kernel_extra=None, min_gain=0.01, log=print):
-    """Energy-estimator ESS/s of the plain sampler and of the learned proposal on one
+    """Energy-estimator ESS/s (energy_ess: per-sweep measurements by default, ESS over the
+    wall time of the measured loop) of the plain sampler and of the learned proposal on one
     system.  Every sampler starts from the same equilibrated paths; a launch is op_runs x
     msteps sweeps followed by one operator measurement per walker and run.
 
@@ -260,8 +284,6 @@ def ess_study(system, beta, N, walkers, S_plain=(3, 4, 5, 6), S_learned=(4, 5, 6
     runs the plain kernel (reported with ``fallback: True``)."""
     from .kernel import PIMCKernel
     from .kernel_args import KernelArgs
-    from .stats import ess, tau_int_batch_means
-
     extra = dict(kernel_extra or {})
 
     def make(S, learned, op_runs_=op_runs, msteps_=msteps):
@@ -295,18 +317,15 @@ def ess_study(system, beta, N, walkers, S_plain=(3, 4, 5, 6), S_learned=(4, 5, 6
 
     def measure(k, label):
         k.setPaths(start_paths)
-        for _ in range(3):
-            k.run()
-        series, t = energy_series(k, launches)
-        e, tau = ess(series)
+        m = energy_ess(k, launches=launches, burn=3)
+        series = m.pop("series")
         info = k.getInfo()
         nodes = walkers * (N // 2 ** k._S) * (2 ** k._S - 1) * op_runs * msteps * launches
-        r = {"S": k._S, "ess": e, "tau_int_launches": tau, "tau_batch_means": tau_int_batch_means(series),
-             "device_s": t, "ess_per_s": e / t, "node_updates_per_s": nodes / t,
-             "acceptance": float(k.getAcceptanceRate()), "energy_mean": float(series.mean()),
-             "energy_se": float(series.mean(axis=0).std() / np.sqrt(walkers)), "registers": int(info.registers)}
-        log(f"{label} S={k._S}: AR {r['acceptance']:.3f} tau {tau:.2f} ESS/s {r['ess_per_s']:.4g} "
-            f"nodes/s {r['node_updates_per_s']:.4g} E {r['energy_mean']:.5f}")
+        r = dict(m, S=k._S, node_updates_per_s=nodes / m["device_s"],
+                 acceptance=float(k.getAcceptanceRate()), energy_mean=float(series.mean()),
+                 energy_se=float(series.mean(axis=0).std() / np.sqrt(walkers)), registers=int(info.registers))
+        log(f"{label} S={k._S}: AR {r['acceptance']:.3f} tau {r['tau_int_sweeps']:.2f} sweeps "
+            f"ESS/s {r['ess_per_s']:.4g} nodes/s {r['node_updates_per_s']:.4g} E {r['energy_mean']:.5f}")
         return r
 
     for S in S_plain:

@@ -38,7 +38,7 @@ def hyperradius2(dof):
     return " + ".join(f"x{i + 1} * x{i + 1}" for i in range(dof))
 
 
-def _kernel(sysm, walkers, N, S, op_runs, msteps, double, accumulation, seed, fast_math):
+def _kernel(sysm, walkers, N, S, op_runs, msteps, double, accumulation, seed, fast_math, min_blocks=0):
     from .kernel import PIMCKernel
     from .kernel_args import KernelArgs
     ka = KernelArgs(system=sysm, nbrOfWalkers=walkers, N=N, beta=sysm.beta, S=S, enableOperator=True,
@@ -47,13 +47,13 @@ def _kernel(sysm, walkers, N, S, op_runs, msteps, double, accumulation, seed, fa
                     enableParallelizePath=True, enableGlobalPath=True, enableGlobalOldPath=False,
                     enableDouble=double, operators=(sysm.energyOp,), correlators=(hyperradius2(sysm.DOF),),
                     operatorRuns=op_runs, metroStepsPerOperatorRun=msteps, accumulation=accumulation,
-                    fastMath=fast_math, seed=seed)
+                    fastMath=fast_math, seed=seed, minBlocksPerSM=min_blocks)
     return PIMCKernel(ka)
 
 
 def precision_study(n_atoms=10, N=1024, walkers=2 ** 20, T=1.0, S=3, op_runs=2, msteps=2, launches=8,
                     fp64_walkers=2 ** 14, n_templates=256, seed=2024, fast_math=True, lags=(0, 1, 2, 4, 8),
-                    burn_in=2, log=None):
+                    burn_in=2, log=None, min_blocks=0):
     """Run the study (``burn_in`` launches of both arms before the measured ones, after
     which the accumulators are zeroed); returns a dict of results (JSON-serialisable)."""
     from .physical_systems.lm2m2 import Lm2m2Cluster
@@ -66,7 +66,7 @@ def precision_study(n_atoms=10, N=1024, walkers=2 ** 20, T=1.0, S=3, op_runs=2, 
     tmpl = sysm.initial_paths(n_templates, N, rng, noise=0.0)
 
     t0 = time.time()
-    k32 = _kernel(sysm, walkers, N, S, op_runs, msteps, False, "study", seed, fast_math)
+    k32 = _kernel(sysm, walkers, N, S, op_runs, msteps, False, "study", seed, fast_math, min_blocks)
     k64 = _kernel(sysm, fp64_walkers, N, S, op_runs, msteps, True, "fp64", seed, fast_math)
     setup_s = time.time() - t0
     k32.setPathsTiled(tmpl.astype(np.float32))

@@ -80,6 +80,14 @@ class ReplicaGroup:
         self._dist.all_reduce(t, op=self._dist.ReduceOp.MAX)
         return float(t.item())
 
+    def sum(self, value: float) -> float:
+        """Sum of a float over the ranks (FP64)."""
+        if not self._dist:
+            return float(value)
+        t = self._tensor([value])
+        self._dist.all_reduce(t, op=self._dist.ReduceOp.SUM)
+        return float(t.item())
+
     def sum_counts(self, counts) -> np.ndarray:
         """Element-wise sum over the ranks of integer counts (histogram and bin counts,
         accepts), exact in int64."""

@@ -66,3 +66,51 @@ def test_autotune_caches(tmp_path):
     assert not r1["cached"] and r1["node_updates_per_s"] > 0
     r2 = autotune(wl, candidates=[(256, 16), (128, 16)], cache_file=cache, launches=1)
     assert r2["cached"] and r2["block_threads"] == r1["block_threads"]
+
+
+def test_batch_systems_match_oracle():
+    """Every system of a small ragged batch (3-6 atoms, different N, T, walker counts and
+    bisection levels) against the oracle run on that system alone with the same paths and
+    xorshift rows (fixed mode).  The batch computes in fast math (__logf, __sinf, __expf)
+    and the oracle with the C library, so a few accept decisions may flip; walkers none of
+    whose work-items flipped must keep the oracle's paths and per-walker energies."""
+    require_gpu()
+    engine()
+    from feynsimul_gb300.batch import BatchSampler
+    from oracle.oracle import OracleConfig, OracleSampler
+    workload = [{"n": 3, "N": 64, "T": 1.0, "walkers": 64}, {"n": 4, "N": 128, "T": 0.7, "walkers": 32},
+                {"n": 5, "N": 64, "T": 1.5, "walkers": 32}, {"n": 6, "N": 32, "T": 0.6, "walkers": 32},
+                {"n": 3, "N": 256, "T": 1.8, "walkers": 32}]
+    op_runs, msteps = 2, 3
+    b = BatchSampler(workload, op_runs=op_runs, msteps=msteps, block_threads=256, tpw_target=16)
+    rng = np.random.RandomState(8)
+    oracles = []
+    for i, w in enumerate(workload):
+        c = b.clusters[w["n"]]
+        S = b.systems[i].bisection_level
+        tpw = w["N"] >> S
+        paths = c.initial_paths(w["walkers"], w["N"], rng).astype(np.float32)
+        ts = rng.randint(0, 2 ** 31 - 1, size=(w["walkers"] * tpw + 1, 4)).astype(np.uint32)
+        ws = rng.randint(0, 2 ** 31 - 1, size=(w["walkers"], 4)).astype(np.uint32)
+        b.set_state(i, paths, ts[:-1], ws)
+        o = OracleSampler(OracleConfig(
+            DOF=c.DOF, potential=c.potential, userCode=c.userCode, nbrOfWalkers=w["walkers"], N=w["N"],
+            beta=float(1.0 / w["T"]), S=S, operatorRuns=op_runs, metroStepsPerOperatorRun=msteps,
+            operators=(c.energyOp,), compat=False, accum=1))
+        o.paths[...] = paths
+        o.seeds[...] = ts
+        o.walker_seeds[...] = ws
+        oracles.append(o)
+    b.run(1, graph=False)
+    for i, (w, o) in enumerate(zip(workload, oracles)):
+        o.run()
+        tpw = w["N"] >> b.systems[i].bisection_level
+        diff = b.accepts(i) != o.accepts
+        assert diff.mean() <= 0.05, (i, diff.mean())
+        keep = ~diff.reshape(w["walkers"], tpw).any(axis=1)
+        assert keep.mean() >= 0.5, (i, keep.mean())
+        np.testing.assert_allclose(b.paths(i)[keep], o.paths[keep], rtol=2e-3, atol=2e-4)
+        e_b = b.energy_sums(i) / (op_runs * w["N"])
+        e_o = o.op_means.reshape(w["walkers"], tpw).mean(axis=1)
+        np.testing.assert_allclose(e_b[keep], e_o[keep], rtol=2e-3, atol=2e-3)
+    b.close()

@@ -7,8 +7,9 @@ the sweep bench.py times -- against the oracle (oracle/pimc_oracle.c).
 (a) IEEE math (fastMath=False), 32 walkers, 2 launches, the oracle's FP32 build on the same
     RANLUX tables: tables bit-exact after every launch, at most one accept decision flipped
     (CUDA's and the C library's log / sin / exp / rsqrt may round differently in the last
-    ulp), and without a flip paths, energy sums and histogram counts equal to the oracle's
-    within rtol 1e-4 (counts: a pair distance within an ulp of a bin edge may change bin).
+    ulp), and without a flip paths (rtol 1e-4), energy sums (rtol 1e-4, atol 1e-4 K: the
+    virial energy cancels pair terms of tens of Kelvin) and histogram counts equal to the
+    oracle's (counts: a pair distance within an ulp of a bin edge may change bin).
 (b) The benchmarked code itself (fastMath=True: __logf / __sinf / __expf), 2048 walkers, one
     launch on the same tables as the oracle's FP32 build: tables still bit-exact, and the
     fraction of work-items whose accept count differs is reported and bounded.
@@ -120,9 +121,12 @@ def test_he3_bench_config_ieee_matches_oracle():
         assert flips <= 1, flips
         if flips == 0:
             np.testing.assert_allclose(k.getPaths(), o.paths, rtol=1e-4, atol=1e-5)
+            # the virial energy is a difference of pair terms of tens of Kelvin (V and
+            # r^2 dV/dr^2), so a work-item's sum carries FP32 rounding of about 1e-6 of
+            # those terms: absolute tolerance 1e-4 K
             raw = k._raw_operators()
-            np.testing.assert_allclose(raw, o.op_means.reshape(-1)[:raw.size], rtol=1e-4, atol=1e-6)
-            np.testing.assert_allclose(k.getOperators(), _oracle_walker_means(o, ka), rtol=1e-4, atol=1e-6)
+            np.testing.assert_allclose(raw, o.op_means.reshape(-1)[:raw.size], rtol=1e-4, atol=1e-4)
+            np.testing.assert_allclose(k.getOperators(), _oracle_walker_means(o, ka), rtol=1e-4, atol=1e-4)
             _, h = k.getHistogram(density=False)
             assert h.sum() == o.hist.sum() or abs(int(h.sum()) - int(o.hist.sum())) <= 4
             assert np.abs(h.astype(np.int64) - o.hist.astype(np.int64)).sum() <= 8
