@@ -67,6 +67,7 @@ struct fs_handle {
     // launch geometry
     int tpw = 1, seg = 1, wpb = 1, block = 1, grid = 1;
     int cor_ilv = 0;  // correlator lags summed in one slice pass over a doubled slice buffer
+    int mx = 1;       // thread groups per CTA: 1 moving + mx - 1 summing correlator lags (FS_MX)
     long long cwstride = 0;  // per-walker correlator buffer in shared memory, elements
     int resident_per_sm = 0;  // resident CTAs per SM of the sweep kernel (fs_run_host), 0 = not yet queried
     long long wstride = 0, vstride = 0;
@@ -321,7 +322,8 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << "\n#define FS_BINS " << (c.enable_bins ? 1 : 0) << "\n#define FS_NHIST " << nhist
       << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n#define FS_GLOBAL " << (c.global_path ? 1 : 0)
       << "\n#define FS_VCACHE " << (h.vstride ? 1 : 0) << "\n#define FS_VSTRIDE " << h.vstride
-      << "\n#define FS_COR_ILV " << h.cor_ilv << "\n#define FS_CWSTRIDE " << h.cwstride << "\n";
+      << "\n#define FS_COR_ILV " << h.cor_ilv << "\n#define FS_CWSTRIDE " << h.cwstride << "\n#define FS_MX "
+      << h.mx << "\n";
     {
         const int mv = c.moves ? c.moves : FS_MOVE_BISECTION;
         const double nb = (double)c.n_slices / c.beta;
@@ -631,7 +633,15 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
         // float-float correlator sums (every mode but the reference's FP32 order, FP32 builds)
         // with at most 4 lags per thread run every lag in one pass over the slice values,
         // stored twice in a row so that slice s1 + tau needs no wrap
-        const long long lpt = (c.n_slices / 2 + h->tpw - 1) / h->tpw;
+        // Correlator helpers: a walker of at most 32 segment threads gets extra threads for
+        // the lag sums, up to 64 lag threads per walker (FS_MX in fs_pimc.cuh).  They need
+        // every CTA full (the walker count a multiple of the walkers per CTA, chosen below).
+        if (!h->cors.empty() && c.enable_parallelize_path && !c.global_path && !c.learned && h->tpw <= 32) {
+            const int lag_threads = std::min(c.n_slices / 2, 64);
+            if (lag_threads > h->tpw) h->mx = lag_threads / h->tpw;
+            if (c.walkers_per_block > 0 && c.n_walkers % c.walkers_per_block) h->mx = 1;
+        }
+        const long long lpt = (c.n_slices / 2 + (long long)h->tpw * h->mx - 1) / ((long long)h->tpw * h->mx);
         h->cor_ilv = (c.accum != 0 && !c.enable_double && lpt <= 4) ? 1 : 0;
         // per-walker stride an odd multiple of 64 bytes: two walkers sharing a warp read
         // opposite bank halves
@@ -665,6 +675,10 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     const size_t hist_bytes = (size_t)(c.hist_bins > 0 && !h->hists.empty() ? c.hist_bins : 0) * 4;
     if (c.walkers_per_block > 0) {
         h->wpb = c.walkers_per_block;
+    } else if (h->mx > 1) {
+        // CTAs of about 128 threads (moving and summing), every CTA full
+        h->wpb = std::max(1, 128 / (h->tpw * h->mx));
+        while (h->wpb > 1 && (c.n_walkers % h->wpb || per_walker * h->wpb + hist_bytes > 100 * 1024)) h->wpb--;
     } else if (h->tpw > 32) {
         h->wpb = 1;
     } else {
@@ -691,7 +705,7 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
         }
         while (c.n_walkers % h->wpb) h->wpb -= wpw;
     }
-    h->block = h->wpb * h->tpw;
+    h->block = h->wpb * h->tpw * h->mx;
     if (h->block > 1024) {
         delete h;
         return fail(nullptr, FS_ERR_CONFIG, "walkers_per_block * threads per walker exceeds 1024");

@@ -23,8 +23,21 @@
 
 #define FS_HALF_N (FS_N / 2)
 #define FS_THREADS (FS_NWALKERS * FS_TPW)
-#define FS_BLOCK (FS_WPB * FS_TPW)
-#define FS_LPT ((FS_HALF_N + FS_TPW - 1) / FS_TPW)  // correlator lags owned per thread
+// Correlator helpers (FS_MX > 1, set by the host for correlator runs whose walkers have few
+// segment threads): the CTA holds FS_MX groups of FS_WPB x FS_TPW threads.  Group 0 runs the
+// moves and the per-slice measurement; every group sums correlator lags, so a walker's N/2
+// lags spread over FS_TPW x FS_MX threads instead of its FS_TPW segment threads.  Each lag is
+// still summed by one thread in slice order, so the sums are the same bit for bit.
+#ifndef FS_MX
+#define FS_MX 1
+#endif
+#define FS_MBLOCK (FS_WPB * FS_TPW)          // threads that run the moves
+#define FS_BLOCK (FS_MBLOCK * FS_MX)
+#define FS_CTPW (FS_TPW * FS_MX)             // correlator threads per walker
+#define FS_LPT ((FS_HALF_N + FS_CTPW - 1) / FS_CTPW)  // correlator lags owned per thread
+#if FS_MX > 1 && (!FS_PARALLEL || FS_TPW > 32 || FS_GLOBAL || FS_NCOR == 0 || FS_NWALKERS % FS_WPB != 0)
+#error "correlator helpers need parallel-path walkers of at most 32 threads in shared memory, correlators, and full CTAs"
+#endif
 #define FS_COR_REGS (FS_ACCUM != 3 && FS_LPT * FS_NCOR <= 16)
 #define FS_CSTEP (FS_N % 4 == 0 ? 4 : 1)  // FP64 correlator: partial sums over s1 mod 4
 // Correlator FP64 sums of FP32 builds (FP64, Kahan and study modes): float-float per
@@ -37,7 +50,7 @@
 #ifndef FS_COR_ILV
 #define FS_COR_ILV 0
 #endif
-#if FS_COR_ILV && !(FS_COR_FF && FS_LPT <= 4 && FS_LPT * FS_TPW <= FS_N)
+#if FS_COR_ILV && !(FS_COR_FF && FS_LPT <= 4 && FS_LPT * FS_CTPW <= FS_N)
 #error "FS_COR_ILV needs float-float correlator sums and at most 4 lags per thread"
 #endif
 #define FS_CSTRIDE (FS_COR_ILV ? 2 * FS_N : FS_N)
@@ -152,6 +165,10 @@ __device__ __forceinline__ fs_u32 fs_offset(FsIStream &g, fs_u32 range)
 #else
 #define FS_MOVE_UNROLL _Pragma("unroll")
 #endif
+// The old- and new-action loops (2^S - 1 potential evaluations each)
+#ifndef FS_ACT_UNROLL
+#define FS_ACT_UNROLL FS_MOVE_UNROLL
+#endif
 
 // kernel.c:258-399 on a shared-memory path P[DOF][N].
 // With the learned proposal (FS_LEARNED) the level-1 midpoint is drawn from N(lmu, lsd^2)
@@ -179,7 +196,7 @@ __device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream 
 #pragma unroll
         for (int d = 0; d < FS_DOF; d++) old[(i - 1) * FS_DOF + d] = FS_AT(P, d, p);
     }
-    FS_MOVE_UNROLL
+    FS_ACT_UNROLL
     for (int i = 1; i < FS_SEG; i++) {
         const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
 #if FS_VCACHE
@@ -236,7 +253,7 @@ __device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream 
         }
     }
     FT aNew = (FT)0;
-    FS_MOVE_UNROLL
+    FS_ACT_UNROLL
     for (int i = 1; i < FS_SEG; i++) {
         const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
         const FT v = fs_pot(FS_ARGS_AT(P, p));
@@ -506,8 +523,11 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     fs_u32 *s_hist = (fs_u32 *)(s_cor + FS_WPB * FS_CWSTRIDE);  // [HBINS]
 
     const int tid_b = threadIdx.x;
-    const int wl = tid_b / FS_TPW;
+    const int grp = tid_b / FS_MBLOCK;             // 0: movers; 1..FS_MX-1: correlator helpers
+    const int wl = (tid_b - grp * FS_MBLOCK) / FS_TPW;
     const int t = tid_b % FS_TPW;
+    const bool mover = FS_MX == 1 || grp == 0;
+    const int lt = grp * FS_TPW + t;               // this thread's lags: lt + j * FS_CTPW
     const int w0 = (blockIdx.x + a.block_offset) * FS_WPB;
     const int w = w0 + wl;
     const int n_here = min(FS_WPB, FS_NWALKERS - w0);
@@ -531,7 +551,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     __syncthreads();
 
     if (active) {
-#if FS_TPW <= 32
+#if FS_TPW <= 32 && FS_MX == 1
         const unsigned lane = threadIdx.x & 31u;
         const unsigned wmask = FS_TPW == 32 ? 0xFFFFFFFFu
                                             : (((1u << FS_TPW) - 1u) << (lane / FS_TPW * FS_TPW));
@@ -552,12 +572,14 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         // ---- RNG state ----
         FsUStream fs;
 #if FS_RANLUX
-        fs_rl_load(fs.st, a.rtab + (size_t)tid * 28);
-        fs.count = 0u;
+        if (mover) {
+            fs_rl_load(fs.st, a.rtab + (size_t)tid * 28);
+            fs.count = 0u;
+        }
         // The walker's offset stream: every reference work-item of the walker advances an
         // identical copy; here one lane advances it in shared memory for the walker.
         FsIStream &is = s_istream[wl];
-        if (t == 0) {
+        if (mover && t == 0) {
 #if FS_COMPAT
             fs_rl_load(is.st, a.gtab + (size_t)tid * 28);
 #else
@@ -568,7 +590,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         FS_WSYNC();
 #else
         FsIStream is;
-        {
+        if (mover) {
             const uint4 s4 = *(const uint4 *)(a.seeds + (size_t)tid * 4);
             fs.x = s4.x; fs.y = s4.y; fs.z = s4.z; fs.w = s4.w;
 #if FS_COMPAT
@@ -604,7 +626,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         for (int c = 0; c < FS_NCOR; c++)
 #pragma unroll
             for (int j = 0; j < FS_LPT; j++) {
-                const int tau = t + j * FS_TPW;
+                const int tau = lt + j * FS_CTPW;
                 cacc[c][j] = tau < FS_HALF_N ? g_cor[c * FS_HALF_N + tau] : (FsCorAcc)0;
             }
 #endif
@@ -619,7 +641,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             const int v_lo = 0, v_hi = FS_N;
 #endif
 #pragma unroll 1
-            for (int s = v_lo; s < v_hi; s++) Vc[FS_PHYS(s)] = fs_pot(FS_ARGS_AT(P, s));
+            for (int s = v_lo; s < (mover ? v_hi : v_lo); s++) Vc[FS_PHYS(s)] = fs_pot(FS_ARGS_AT(P, s));
         }
         FS_WSYNC();
 #endif
@@ -649,11 +671,11 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #endif
 #if FS_BISECT
 #if FS_RANLUX
-                if (t == 0) s_off[wl] = fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N);
+                if (mover && t == 0) s_off[wl] = fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N);
                 FS_WSYNC();
                 const fs_u32 off = s_off[wl];
 #else
-                const fs_u32 off = fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N);
+                const fs_u32 off = mover ? fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N) : 0u;
 #endif
 #if FS_PARALLEL
                 const fs_u32 start = (off + (fs_u32)(FS_SEG * t)) & (FS_N - 1);
@@ -690,7 +712,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                 }
                 n_acc += (fs_u32)fs_bisect(P, Vc, start, fs, sigma, lmu, lsd);
 #else
-                n_acc += (fs_u32)fs_bisect(P, Vc, start, fs, sigma, nullptr, nullptr);
+                if (mover) n_acc += (fs_u32)fs_bisect(P, Vc, start, fs, sigma, nullptr, nullptr);
 #endif
 #endif  // FS_BISECT
                 FS_WSYNC();
@@ -702,7 +724,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             const int s_lo = 0, s_hi = FS_N;
 #endif
 #pragma unroll 1
-            for (int s = s_lo; s < s_hi; s++) {
+            for (int s = s_lo; s < (mover ? s_hi : s_lo); s++) {
 #if FS_NOPS > 0
                 FT ov[FS_NOPS];
                 fs_ops(FS_ARGS_AT(P, s), ov);
@@ -764,7 +786,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             }
 #if FS_NCOR > 0
             FS_WSYNC();
-            // lags tau = t + j*TPW owned by this thread
+            // lags tau = lt + j * FS_CTPW owned by this thread
 #pragma unroll
             for (int c = 0; c < FS_NCOR; c++) {
                 const FT *Cc = C + c * FS_CSTRIDE;
@@ -775,7 +797,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                 // a full unroll, 0.81 ms, misses the instruction cache); by 2 in the study mode,
                 // whose three sums per product make the loop body large (10-atom cluster: 2.08
                 // against 1.80-1.87e9 node updates/s at 8).  Lags past N/2 (when
-                // FS_TPW does not divide N/2) are summed and dropped; s1 + tau < N + LPT * TPW
+                // FS_CTPW does not divide N/2) are summed and dropped; s1 + tau < N + LPT * CTPW
                 // <= 2N stays inside the doubled slice values.
                 {
                     float fs[FS_LPT], fe[FS_LPT];
@@ -787,7 +809,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                         fs[j] = 0.0f;
                         fe[j] = 0.0f;
 #if FS_ACCUM == 3
-                        const int tau = t + j * FS_TPW;
+                        const int tau = lt + j * FS_CTPW;
                         const FsCorAcc a0 = tau < FS_HALF_N ? g_cor[c * FS_HALF_N + tau] : FsCorAcc{};
                         af[j] = a0.f; aks[j] = a0.ks; akc[j] = a0.kc;
 #endif
@@ -801,7 +823,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                         const FT c0 = Cc[s1];
 #pragma unroll
                         for (int j = 0; j < FS_LPT; j++) {
-                            const FT q = FS_MUL(c0, Cc[s1 + t + j * FS_TPW]);
+                            const FT q = FS_MUL(c0, Cc[s1 + lt + j * FS_CTPW]);
                             fs_ff_add(fs[j], fe[j], q);
 #if FS_ACCUM == 3
                             af[j] = __fadd_rn(af[j], q);
@@ -815,7 +837,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #if FS_COR_REGS
                         cacc[c][j] = __dadd_rn(cacc[c][j], m);
 #else
-                        const int tau = t + j * FS_TPW;
+                        const int tau = lt + j * FS_CTPW;
                         if (tau < FS_HALF_N) {
 #if FS_ACCUM == 3
                             FsCorAcc *g = g_cor + c * FS_HALF_N + tau;
@@ -835,7 +857,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #pragma unroll 1
 #endif
                 for (int j = 0; j < FS_LPT; j++) {
-                    const int tau = t + j * FS_TPW;
+                    const int tau = lt + j * FS_CTPW;
                     if (tau >= FS_HALF_N) continue;
 #if FS_COR_REGS
                     FsCorAcc acc = cacc[c][j];
@@ -932,10 +954,10 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         }
 
         // ---- epilogue (kernel.c:801-836) ----
-        a.accepts[tid] = n_acc;
+        if (mover) a.accepts[tid] = n_acc;
 #if FS_NOPS > 0
 #pragma unroll
-        for (int i = 0; i < FS_NOPS; i++) {
+        for (int i = 0; i < (mover ? FS_NOPS : 0); i++) {
             const size_t o = (size_t)tid * FS_NOPS + i;
 #if FS_ACCUM == 0
             ((FT *)a.op_means)[o] = FS_MUL(opr[i], (FT)FS_OPNORM);
@@ -955,7 +977,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         for (int c = 0; c < FS_NCOR; c++)
 #pragma unroll
             for (int j = 0; j < FS_LPT; j++) {
-                const int tau = t + j * FS_TPW;
+                const int tau = lt + j * FS_CTPW;
                 if (tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = cacc[c][j];
             }
 #endif
@@ -977,17 +999,17 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         }
 #endif
 #if FS_RANLUX
-        fs_rl_store(fs.st, a.rtab + (size_t)tid * 28);
+        if (mover) fs_rl_store(fs.st, a.rtab + (size_t)tid * 28);
         FS_WSYNC();
 #if FS_COMPAT
-        fs_rl_store(is.st, a.gtab + (size_t)tid * 28);
+        if (mover) fs_rl_store(is.st, a.gtab + (size_t)tid * 28);
 #else
-        if (t == 0) fs_rl_store(is.st, a.gtab + (size_t)w * 28);
+        if (mover && t == 0) fs_rl_store(is.st, a.gtab + (size_t)w * 28);
 #endif
 #else
-        *(uint4 *)(a.seeds + (size_t)tid * 4) = make_uint4(fs.x, fs.y, fs.z, fs.w);
+        if (mover) *(uint4 *)(a.seeds + (size_t)tid * 4) = make_uint4(fs.x, fs.y, fs.z, fs.w);
 #if !FS_COMPAT
-        if (t == 0) *(uint4 *)(a.walker_seeds + (size_t)w * 4) = make_uint4(is.x, is.y, is.z, is.w);
+        if (mover && t == 0) *(uint4 *)(a.walker_seeds + (size_t)w * 4) = make_uint4(is.x, is.y, is.z, is.w);
 #endif
 #endif
 #undef FS_WSYNC
