@@ -406,20 +406,6 @@ __global__ void fs_mlp_pack_kernel(const float *params, fs_bf16 *wq, uint2 *frag
     }
 }
 
-// inference on rows of 16 features (the sampler's device function, one row per thread)
-__global__ void __launch_bounds__(128) fs_mlp_infer_kernel(const uint2 *frag, const float *bias, const float *x,
-                                                           float *y, int n_rows)
-{
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    float xi[16], yo[16];
-#pragma unroll
-    for (int c = 0; c < 16; c++) xi[c] = row < n_rows ? x[(size_t)row * 16 + c] : 0.f;
-    fs_mlp_eval_warp(frag, bias, xi, yo);  // all lanes take part
-    if (row < n_rows)
-#pragma unroll
-        for (int c = 0; c < 16; c++) y[(size_t)row * 16 + c] = yo[c];
-}
-
 // ------------------------------------------------------------------ C ABI
 static int launch_check(const char *what)
 {
@@ -474,11 +460,13 @@ extern "C" int fs_mlp_pack(const float *params, uint16_t *wq, void *frag, float 
     return launch_check("fs_mlp_pack_kernel");
 }
 
+// batched inference on the tcgen05 tensor cores (fs_mlp_tc.cu)
+extern int fsi_mlp_infer_tc(const void *frag, const float *bias, const float *x, float *y, int n_rows,
+                            cudaStream_t s);
+
 extern "C" int fs_mlp_infer(const void *frag, const float *bias, const float *x, float *y, int32_t n_rows,
                             void *stream)
 {
     if (n_rows < 1) return FS_OK;
-    fs_mlp_infer_kernel<<<(n_rows + 127) / 128, 128, 0, (cudaStream_t)stream>>>((const uint2 *)frag, bias, x, y,
-                                                                                n_rows);
-    return launch_check("fs_mlp_infer_kernel");
+    return fsi_mlp_infer_tc(frag, bias, x, y, n_rows, (cudaStream_t)stream);
 }

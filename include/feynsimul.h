@@ -293,7 +293,10 @@ int fs_mlp_adam(float *params, float *m, float *v, float *grad, uint16_t *wq, in
                 float lr, void *stream);
 /* params -> BF16 training copy, inference fragments (n_frag_u2 x 8 bytes), biases. */
 int fs_mlp_pack(const float *params, uint16_t *wq, void *frag, float *bias, void *stream);
-/* Inference of rows x[n][16] -> y[n][16] with the sampler's device code. */
+/* Inference of rows x[n][16] -> y[n][16] on the tcgen05 tensor cores (BF16 operands in
+ * shared memory, FP32 accumulators in tensor memory), rounding to BF16 at the same points as
+ * the sampler's device code (inputs, weights, post-ReLU activations).  A CTA whose bounded
+ * wait for the tensor cores runs out writes NaN to its rows. */
 int fs_mlp_infer(const void *frag, const float *bias, const float *x, float *y, int32_t n_rows,
                  void *stream);
 /* Load a packed model (host buffers) into a handle created with cfg.learned = 1;

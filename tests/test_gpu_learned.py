@@ -51,16 +51,26 @@ def test_pack_matches_host_layout():
     assert np.array_equal(tq.cpu().numpy().view(np.uint16), want_q)
 
 
-def test_inference_matches_oracle():
+@pytest.mark.parametrize("n_rows", [1000, 128, 1, 300 * 128 + 77])
+def test_inference_matches_oracle(n_rows):
+    """Batched inference on the tcgen05 tensor cores (fs_mlp_infer) against the FP64 oracle
+    that rounds to BF16 at the same points.  Only the FP32 accumulation order differs, which
+    can move a hidden activation across a BF16 rounding boundary (one BF16 ulp, 2^-8
+    relative, for that element), so outputs agree to about 1% of their scale; the median
+    error is far smaller.  Row counts: a partial tile, one full tile, a single row, and more
+    tiles than resident CTAs (the persistent loop)."""
     from feynsimul_gb300.learned import LearnedProposal
     from oracle import mlp_oracle
     p = _rand_params(5, out_scale=0.3)
     m = LearnedProposal(6, 0.2, 1.0, params=p)
-    x = np.random.RandomState(1).randn(1000, 16).astype(np.float32)
+    x = np.random.RandomState(1).randn(n_rows, 16).astype(np.float32)
     x[:, 12:] = 0
     y = m.predict(x)
+    assert np.all(np.isfinite(y))
     _, _, _, z4 = mlp_oracle.forward(p, x)
-    np.testing.assert_allclose(y, z4, rtol=2e-2, atol=2e-2 * np.abs(z4).max())
+    scale = np.abs(z4).max()
+    np.testing.assert_allclose(y, z4, rtol=1e-2, atol=1e-2 * scale)
+    assert np.median(np.abs(y - z4)) < 1e-3 * scale
 
 
 def test_gradients_match_oracle():
