@@ -321,7 +321,7 @@ def learned_study(quick=True):
     t0 = time.perf_counter()
     res = ess_study(sysm, sysm.beta, 256, 16384,
                     S_plain=(4, 5) if quick else (3, 4, 5, 6), S_learned=(4, 5) if quick else (4, 5, 6, 7),
-                    launches=200, train_steps=1500 if quick else 3000,
+                    launches=200, train_steps=1500 if quick else 3000, force_network=(4,) if quick else (4, 5, 6, 7),
                     kernel_extra=dict(enableRanlux=True, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
                                       walkersPerBlock=TUNED_WPB["he3"], minBlocksPerSM=TUNED_MIN_BLOCKS["he3"]),
                     log=lambda *a: None)
@@ -332,7 +332,9 @@ def learned_study(quick=True):
            "learned": {str(k): {kk: v[kk] for kk in ("acceptance", "tau_int_sweeps", "ess_per_s",
                                                       "node_updates_per_s", "loss_start", "loss_end",
                                                       "validation_gain_nats", "fallback")}
-                       for k, v in res["learned"].items()}}
+                       for k, v in res["learned"].items()},
+           "forced": {str(k): {kk: v[kk] for kk in ("acceptance", "tau_int_sweeps", "ess_per_s", "node_updates_per_s",
+                                                     "validation_gain_nats")} for k, v in res.get("forced", {}).items()}}
     if not quick:
         out["coarse_ho"] = coarse_ho_gain()
     return out

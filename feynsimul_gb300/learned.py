@@ -272,11 +272,14 @@ def energy_ess(kernel, launches=200, burn=10):
 
 def ess_study(system, beta, N, walkers, S_plain=(3, 4, 5, 6), S_learned=(4, 5, 6, 7), launches=200,
               op_runs=1, msteps=1, burn=10, train_steps=3000, harvest_snapshots=4, seed=1,
-              kernel_extra=None, min_gain=0.01, log=print):
+              kernel_extra=None, min_gain=0.01, force_network=(), log=print):
     """Energy-estimator ESS/s (energy_ess: per-sweep measurements by default, ESS over the
     wall time of the measured loop) of the plain sampler and of the learned proposal on one
     system.  Every sampler starts from the same equilibrated paths; a launch is op_runs x
     msteps sweeps followed by one operator measurement per walker and run.
+
+    ``force_network``: levels S whose network is also measured when the gate rejects it
+    (reported under ``results["forced"]``), so the network's own ESS/s is known.
 
     The learned sampler keeps the plain bisection as its fallback: a network whose held-out
     log-likelihood gain over the free bridge (LearnedProposal.validation_gain, on 10% of the
@@ -346,6 +349,11 @@ def ess_study(system, beta, N, walkers, S_plain=(3, 4, 5, 6), S_learned=(4, 5, 6
         gain = model.validation_gain(feats[:n_val], z[:n_val])
         info = dict(train_samples=int(feats.shape[0] - n_val), loss_start=float(hist[:20].mean()),
                     loss_end=float(hist[-50:].mean()), validation_gain_nats=gain)
+        if gain < min_gain and S in force_network:
+            k = make(S, True)
+            k.setLearnedProposal(model)
+            results.setdefault("forced", {})[S] = dict(measure(k, "forced "), fallback=False, **info)
+            k.close()
         if gain < min_gain:
             if S not in results["plain"]:
                 k = make(S, False)
@@ -374,5 +382,10 @@ def ess_study(system, beta, N, walkers, S_plain=(3, 4, 5, 6), S_learned=(4, 5, 6
         "learned_vs_best_plain": best_learned["ess_per_s"] / best_plain["ess_per_s"],
         "network_levels_used": sorted(int(r["S"]) for r in used),
         "network_only_vs_best_plain": (best_net["ess_per_s"] / best_plain["ess_per_s"]) if best_net else None,
+        "network_forced": {int(S): {"ess_per_s": r["ess_per_s"], "acceptance": r["acceptance"],
+                                    "tau_int_sweeps": r["tau_int_sweeps"],
+                                    "vs_plain_same_S": r["ess_per_s"] / results["plain"][S]["ess_per_s"]
+                                    if S in results["plain"] else None}
+                           for S, r in results.get("forced", {}).items()},
         "validation_gain_nats": {int(S): r["validation_gain_nats"] for S, r in results["learned"].items()}}
     return results
