@@ -48,12 +48,12 @@ def _he3():
     return Lm2m2Cluster(3, 1.0)
 
 
-def _he3_ka(sysm, walkers, op_runs, msteps):
+def _he3_ka(sysm, walkers, op_runs, msteps, lux=2):
     return dict(nbrOfWalkers=walkers, N=256, beta=float(sysm.beta), S=4, enableOperator=True,
                 enableCorrelator=False, enableBisection=True, enablePathShift=False,
                 enableSingleNodeMove=False, enableBins=False, nbrOfWalkersPerWorkGroup=1,
                 enableParallelizePath=True, enableGlobalPath=False, enableGlobalOldPath=False,
-                enableDouble=False, enableRanlux=True, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
+                enableDouble=False, enableRanlux=True, luxuaryFactor=lux, ranluxIntMax=2 ** 32 - 1,
                 operators=(sysm.energyOp,), operatorRuns=op_runs, metroStepsPerOperatorRun=msteps)
 
 
@@ -96,9 +96,13 @@ def _same_tables(k, o):
 
 
 # ------------------------------------------------------------------------- (a)
-def test_he3_bench_config_ieee_matches_oracle():
+@pytest.mark.parametrize("lux", [2, 0, 1, 3])
+def test_he3_bench_config_ieee_matches_oracle(lux):
+    """lux 2 is the benchmarked luxury; 0, 1 and 3 (skips of 24, 76 and 380 steps per 24
+    outputs, the first in the per-cycle scheme) take the generator's other branches, whose
+    12-value draws of the six-DOF move run as single blocks or as four-value calls."""
     sysm = _he3()
-    ka = _he3_ka(sysm, walkers=32, op_runs=2, msteps=5)
+    ka = _he3_ka(sysm, walkers=32, op_runs=2, msteps=5, lux=lux)
     k = _gpu_kernel(sysm, ka, seed=3, fast=False)
     o = _oracle(sysm, ka, double=False)
     p0 = sysm.initial_paths(32, 256, np.random.RandomState(11)).astype(np.float32)
