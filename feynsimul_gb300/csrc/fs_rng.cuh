@@ -168,21 +168,15 @@ __device__ __forceinline__ void fs_rl_cycle(FsRanlux &r)
         : "+r"(r.s[0]), "+r"(r.s[1]), "+r"(r.s[2]), "+r"(r.s[3]), "+r"(r.s[4]), "+r"(r.s[5]), "+r"(r.s[6]), "+r"(r.s[7]), "+r"(r.s[8]), "+r"(r.s[9]), "+r"(r.s[10]), "+r"(r.s[11]), "+r"(r.s[12]), "+r"(r.s[13]), "+r"(r.s[14]), "+r"(r.s[15]), "+r"(r.s[16]), "+r"(r.s[17]), "+r"(r.s[18]), "+r"(r.s[19]), "+r"(r.s[20]), "+r"(r.s[21]), "+r"(r.s[22]), "+r"(r.s[23]), "+r"(r.carry));
 }
 
-// output of the step that just updated lag A (pyopencl-ranluxcl.cl:363-378); A must fold to
-// a constant where it is inlined, so the lags stay in registers
-__device__ __forceinline__ float fs_rl_value_at(const FsRanlux &r, int A)
+// output of the step that just updated lag A (pyopencl-ranluxcl.cl:363-378)
+template <int A>
+__device__ __forceinline__ float fs_rl_value(const FsRanlux &r)
 {
     const fs_u32 v = r.s[A];
     const float hi = __fmul_rn(__uint2float_rn(v), 0x1p-32f);
     const float lo = __fmul_rn(__uint2float_rn(r.s[(A + 9) % 24]), 0x1p-56f);
     float out = v < (4096u << 8) ? __fadd_rn(hi, lo) : hi;
     return out == 0.0f ? 0x1p-48f : out;
-}
-
-template <int A>
-__device__ __forceinline__ float fs_rl_value(const FsRanlux &r)
-{
-    return fs_rl_value_at(r, A);
 }
 
 // NSKIP steps starting at cycle position pos (a multiple of 4); returns the new position
@@ -308,192 +302,6 @@ __device__ __forceinline__ void fs_rl_store(const FsRanlux &r, fs_u32 *t)
     t[27] = r.stepnr;
 }
 
-// Twelve consecutive steps (three 4-step chunks) starting at cycle position P as one borrow
-// chain: one carry hand-over instead of three.  Generated for P = 0, 4, ..., 20; position q
-// updates lag 23 - q from lag (33 - q) mod 24, as fs_rl_cycle does.
-__device__ __forceinline__ void fs_rl_chunk12_p0(FsRanlux &r)
-{
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %12;\n\t"
-        "subc.cc.u32 %0, %13, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
-        "subc.cc.u32 %1, %14, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
-        "subc.cc.u32 %2, %15, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
-        "subc.cc.u32 %3, %16, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "subc.cc.u32 %4, %17, %4;\n\t" "and.b32 %4, %4, -256;\n\t"
-        "subc.cc.u32 %5, %18, %5;\n\t" "and.b32 %5, %5, -256;\n\t"
-        "subc.cc.u32 %6, %19, %6;\n\t" "and.b32 %6, %6, -256;\n\t"
-        "subc.cc.u32 %7, %20, %7;\n\t" "and.b32 %7, %7, -256;\n\t"
-        "subc.cc.u32 %8, %21, %8;\n\t" "and.b32 %8, %8, -256;\n\t"
-        "subc.cc.u32 %9, %22, %9;\n\t" "and.b32 %9, %9, -256;\n\t"
-        "subc.cc.u32 %10, %0, %10;\n\t" "and.b32 %10, %10, -256;\n\t"
-        "subc.cc.u32 %11, %1, %11;\n\t" "and.b32 %11, %11, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %12, fsz, fsz;\n\t" "}"
-        : "+r"(r.s[23]), "+r"(r.s[22]), "+r"(r.s[21]), "+r"(r.s[20]), "+r"(r.s[19]), "+r"(r.s[18]), "+r"(r.s[17]), "+r"(r.s[16]), "+r"(r.s[15]), "+r"(r.s[14]), "+r"(r.s[13]), "+r"(r.s[12]), "+r"(r.carry)
-        : "r"(r.s[9]), "r"(r.s[8]), "r"(r.s[7]), "r"(r.s[6]), "r"(r.s[5]), "r"(r.s[4]), "r"(r.s[3]), "r"(r.s[2]), "r"(r.s[1]), "r"(r.s[0]));
-}
-
-__device__ __forceinline__ void fs_rl_chunk12_p4(FsRanlux &r)
-{
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %12;\n\t"
-        "subc.cc.u32 %0, %13, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
-        "subc.cc.u32 %1, %14, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
-        "subc.cc.u32 %2, %15, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
-        "subc.cc.u32 %3, %16, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "subc.cc.u32 %4, %17, %4;\n\t" "and.b32 %4, %4, -256;\n\t"
-        "subc.cc.u32 %5, %18, %5;\n\t" "and.b32 %5, %5, -256;\n\t"
-        "subc.cc.u32 %6, %19, %6;\n\t" "and.b32 %6, %6, -256;\n\t"
-        "subc.cc.u32 %7, %20, %7;\n\t" "and.b32 %7, %7, -256;\n\t"
-        "subc.cc.u32 %8, %21, %8;\n\t" "and.b32 %8, %8, -256;\n\t"
-        "subc.cc.u32 %9, %22, %9;\n\t" "and.b32 %9, %9, -256;\n\t"
-        "subc.cc.u32 %10, %0, %10;\n\t" "and.b32 %10, %10, -256;\n\t"
-        "subc.cc.u32 %11, %1, %11;\n\t" "and.b32 %11, %11, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %12, fsz, fsz;\n\t" "}"
-        : "+r"(r.s[19]), "+r"(r.s[18]), "+r"(r.s[17]), "+r"(r.s[16]), "+r"(r.s[15]), "+r"(r.s[14]), "+r"(r.s[13]), "+r"(r.s[12]), "+r"(r.s[11]), "+r"(r.s[10]), "+r"(r.s[9]), "+r"(r.s[8]), "+r"(r.carry)
-        : "r"(r.s[5]), "r"(r.s[4]), "r"(r.s[3]), "r"(r.s[2]), "r"(r.s[1]), "r"(r.s[0]), "r"(r.s[23]), "r"(r.s[22]), "r"(r.s[21]), "r"(r.s[20]));
-}
-
-__device__ __forceinline__ void fs_rl_chunk12_p8(FsRanlux &r)
-{
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %12;\n\t"
-        "subc.cc.u32 %0, %13, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
-        "subc.cc.u32 %1, %14, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
-        "subc.cc.u32 %2, %15, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
-        "subc.cc.u32 %3, %16, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "subc.cc.u32 %4, %17, %4;\n\t" "and.b32 %4, %4, -256;\n\t"
-        "subc.cc.u32 %5, %18, %5;\n\t" "and.b32 %5, %5, -256;\n\t"
-        "subc.cc.u32 %6, %19, %6;\n\t" "and.b32 %6, %6, -256;\n\t"
-        "subc.cc.u32 %7, %20, %7;\n\t" "and.b32 %7, %7, -256;\n\t"
-        "subc.cc.u32 %8, %21, %8;\n\t" "and.b32 %8, %8, -256;\n\t"
-        "subc.cc.u32 %9, %22, %9;\n\t" "and.b32 %9, %9, -256;\n\t"
-        "subc.cc.u32 %10, %0, %10;\n\t" "and.b32 %10, %10, -256;\n\t"
-        "subc.cc.u32 %11, %1, %11;\n\t" "and.b32 %11, %11, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %12, fsz, fsz;\n\t" "}"
-        : "+r"(r.s[15]), "+r"(r.s[14]), "+r"(r.s[13]), "+r"(r.s[12]), "+r"(r.s[11]), "+r"(r.s[10]), "+r"(r.s[9]), "+r"(r.s[8]), "+r"(r.s[7]), "+r"(r.s[6]), "+r"(r.s[5]), "+r"(r.s[4]), "+r"(r.carry)
-        : "r"(r.s[1]), "r"(r.s[0]), "r"(r.s[23]), "r"(r.s[22]), "r"(r.s[21]), "r"(r.s[20]), "r"(r.s[19]), "r"(r.s[18]), "r"(r.s[17]), "r"(r.s[16]));
-}
-
-__device__ __forceinline__ void fs_rl_chunk12_p12(FsRanlux &r)
-{
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %12;\n\t"
-        "subc.cc.u32 %0, %13, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
-        "subc.cc.u32 %1, %14, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
-        "subc.cc.u32 %2, %15, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
-        "subc.cc.u32 %3, %16, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "subc.cc.u32 %4, %17, %4;\n\t" "and.b32 %4, %4, -256;\n\t"
-        "subc.cc.u32 %5, %18, %5;\n\t" "and.b32 %5, %5, -256;\n\t"
-        "subc.cc.u32 %6, %19, %6;\n\t" "and.b32 %6, %6, -256;\n\t"
-        "subc.cc.u32 %7, %20, %7;\n\t" "and.b32 %7, %7, -256;\n\t"
-        "subc.cc.u32 %8, %21, %8;\n\t" "and.b32 %8, %8, -256;\n\t"
-        "subc.cc.u32 %9, %22, %9;\n\t" "and.b32 %9, %9, -256;\n\t"
-        "subc.cc.u32 %10, %0, %10;\n\t" "and.b32 %10, %10, -256;\n\t"
-        "subc.cc.u32 %11, %1, %11;\n\t" "and.b32 %11, %11, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %12, fsz, fsz;\n\t" "}"
-        : "+r"(r.s[11]), "+r"(r.s[10]), "+r"(r.s[9]), "+r"(r.s[8]), "+r"(r.s[7]), "+r"(r.s[6]), "+r"(r.s[5]), "+r"(r.s[4]), "+r"(r.s[3]), "+r"(r.s[2]), "+r"(r.s[1]), "+r"(r.s[0]), "+r"(r.carry)
-        : "r"(r.s[21]), "r"(r.s[20]), "r"(r.s[19]), "r"(r.s[18]), "r"(r.s[17]), "r"(r.s[16]), "r"(r.s[15]), "r"(r.s[14]), "r"(r.s[13]), "r"(r.s[12]));
-}
-
-__device__ __forceinline__ void fs_rl_chunk12_p16(FsRanlux &r)
-{
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %12;\n\t"
-        "subc.cc.u32 %0, %13, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
-        "subc.cc.u32 %1, %14, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
-        "subc.cc.u32 %2, %15, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
-        "subc.cc.u32 %3, %16, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "subc.cc.u32 %4, %17, %4;\n\t" "and.b32 %4, %4, -256;\n\t"
-        "subc.cc.u32 %5, %18, %5;\n\t" "and.b32 %5, %5, -256;\n\t"
-        "subc.cc.u32 %6, %19, %6;\n\t" "and.b32 %6, %6, -256;\n\t"
-        "subc.cc.u32 %7, %20, %7;\n\t" "and.b32 %7, %7, -256;\n\t"
-        "subc.cc.u32 %8, %21, %8;\n\t" "and.b32 %8, %8, -256;\n\t"
-        "subc.cc.u32 %9, %22, %9;\n\t" "and.b32 %9, %9, -256;\n\t"
-        "subc.cc.u32 %10, %0, %10;\n\t" "and.b32 %10, %10, -256;\n\t"
-        "subc.cc.u32 %11, %1, %11;\n\t" "and.b32 %11, %11, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %12, fsz, fsz;\n\t" "}"
-        : "+r"(r.s[7]), "+r"(r.s[6]), "+r"(r.s[5]), "+r"(r.s[4]), "+r"(r.s[3]), "+r"(r.s[2]), "+r"(r.s[1]), "+r"(r.s[0]), "+r"(r.s[23]), "+r"(r.s[22]), "+r"(r.s[21]), "+r"(r.s[20]), "+r"(r.carry)
-        : "r"(r.s[17]), "r"(r.s[16]), "r"(r.s[15]), "r"(r.s[14]), "r"(r.s[13]), "r"(r.s[12]), "r"(r.s[11]), "r"(r.s[10]), "r"(r.s[9]), "r"(r.s[8]));
-}
-
-__device__ __forceinline__ void fs_rl_chunk12_p20(FsRanlux &r)
-{
-    asm("{\n\t.reg .u32 fsz;\n\tmov.u32 fsz, 0;\n\t" "sub.cc.u32 fsz, fsz, %12;\n\t"
-        "subc.cc.u32 %0, %13, %0;\n\t" "and.b32 %0, %0, -256;\n\t"
-        "subc.cc.u32 %1, %14, %1;\n\t" "and.b32 %1, %1, -256;\n\t"
-        "subc.cc.u32 %2, %15, %2;\n\t" "and.b32 %2, %2, -256;\n\t"
-        "subc.cc.u32 %3, %16, %3;\n\t" "and.b32 %3, %3, -256;\n\t"
-        "subc.cc.u32 %4, %17, %4;\n\t" "and.b32 %4, %4, -256;\n\t"
-        "subc.cc.u32 %5, %18, %5;\n\t" "and.b32 %5, %5, -256;\n\t"
-        "subc.cc.u32 %6, %19, %6;\n\t" "and.b32 %6, %6, -256;\n\t"
-        "subc.cc.u32 %7, %20, %7;\n\t" "and.b32 %7, %7, -256;\n\t"
-        "subc.cc.u32 %8, %21, %8;\n\t" "and.b32 %8, %8, -256;\n\t"
-        "subc.cc.u32 %9, %22, %9;\n\t" "and.b32 %9, %9, -256;\n\t"
-        "subc.cc.u32 %10, %0, %10;\n\t" "and.b32 %10, %10, -256;\n\t"
-        "subc.cc.u32 %11, %1, %11;\n\t" "and.b32 %11, %11, -256;\n\t"
-        "mov.u32 fsz, 0;\n\t" "subc.u32 %12, fsz, fsz;\n\t" "}"
-        : "+r"(r.s[3]), "+r"(r.s[2]), "+r"(r.s[1]), "+r"(r.s[0]), "+r"(r.s[23]), "+r"(r.s[22]), "+r"(r.s[21]), "+r"(r.s[20]), "+r"(r.s[19]), "+r"(r.s[18]), "+r"(r.s[17]), "+r"(r.s[16]), "+r"(r.carry)
-        : "r"(r.s[13]), "r"(r.s[12]), "r"(r.s[11]), "r"(r.s[10]), "r"(r.s[9]), "r"(r.s[8]), "r"(r.s[7]), "r"(r.s[6]), "r"(r.s[5]), "r"(r.s[4]));
-}
-
-template <int P> __device__ __forceinline__ void fs_rl_chunk12(FsRanlux &r);
-template <> __device__ __forceinline__ void fs_rl_chunk12<0>(FsRanlux &r) { fs_rl_chunk12_p0(r); }
-template <> __device__ __forceinline__ void fs_rl_chunk12<4>(FsRanlux &r) { fs_rl_chunk12_p4(r); }
-template <> __device__ __forceinline__ void fs_rl_chunk12<8>(FsRanlux &r) { fs_rl_chunk12_p8(r); }
-template <> __device__ __forceinline__ void fs_rl_chunk12<12>(FsRanlux &r) { fs_rl_chunk12_p12(r); }
-template <> __device__ __forceinline__ void fs_rl_chunk12<16>(FsRanlux &r) { fs_rl_chunk12_p16(r); }
-template <> __device__ __forceinline__ void fs_rl_chunk12<20>(FsRanlux &r) { fs_rl_chunk12_p20(r); }
-
-// The twelve outputs of a 12-step block from position P: the plain conversion, and the
-// small-value correction of fs_rl_value for all twelve when some lane drew a value below
-// 2^-12.  Deferring the correction to the end of the block is exact: an output's correction
-// lag, (A + 9) mod 24 for output lag A, is not among the lags the block's later steps update.
-template <int P>
-__device__ __forceinline__ void fs_rl_out12(FsRanlux &r, float (&o)[12])
-{
-    fs_rl_chunk12<P>(r);
-    fs_u32 mn = 0xFFFFFFFFu;
-#pragma unroll
-    for (int j = 0; j < 12; j++) {
-        const fs_u32 v = r.s[(47 - P - j) % 24];
-        o[j] = __fmul_rn(__uint2float_rn(v), 0x1p-32f);
-        mn = min(mn, v);
-    }
-    if (__any_sync(__activemask(), mn < (4096u << 8))) {
-#pragma unroll
-        for (int j = 0; j < 12; j++) o[j] = fs_rl_value_at(r, (47 - P - j) % 24);
-    }
-}
-
-// Twelve outputs as three fs_rl_next4 calls would give them, in one block when no skip
-// falls inside: in the per-24-outputs scheme (NSKIP not a multiple of 24) when at most 12
-// outputs have been taken since the last skip, in the per-cycle scheme when the block does
-// not cross the cycle boundary (always without skips).  Returns false when the caller must
-// take the four-value path instead.
-template <int NSKIP>
-__device__ __forceinline__ bool fs_rl_next12(FsRanlux &r, float (&o)[12])
-{
-    const bool fast = NSKIP == 0 ? true : (NSKIP % 24 != 0 ? r.in24 <= 12u : r.stepnr <= 12u);
-    if (!fast) return false;
-    switch (r.stepnr) {
-    case 0: fs_rl_out12<0>(r, o); break;
-    case 4: fs_rl_out12<4>(r, o); break;
-    case 8: fs_rl_out12<8>(r, o); break;
-    case 12: fs_rl_out12<12>(r, o); break;
-    case 16: fs_rl_out12<16>(r, o); break;
-    default: fs_rl_out12<20>(r, o); break;
-    }
-    fs_u32 pos = r.stepnr + 12u;
-    if (NSKIP % 24 == 0) {
-        // per-cycle scheme: skip when a cycle completes; in24 stays untouched
-        if (pos >= 24u) pos = NSKIP == 0 ? pos - 24u : fs_rl_skip<NSKIP>(r, 0u);
-        r.stepnr = pos;
-    } else {
-        r.stepnr = pos >= 24u ? pos - 24u : pos;
-        r.in24 += 12u;
-        if (r.in24 == 24u) {
-            r.in24 = 0u;
-            r.stepnr = fs_rl_skip<NSKIP>(r, r.stepnr);
-        }
-    }
-    return true;
-}
-
 // kernel.c:180-190: four buffered values per generator call; the counter starts at 0
 // in every launch (kernel.c:557-558)
 template <int NSKIP>
@@ -521,31 +329,13 @@ struct FsRanluxStream {
         // one inlined generator call in a rolled loop (the generator is large; K/4 inlined
         // copies cost instruction-cache misses): each quadruple is shifted in at the end
         float c[K];
-        if (K == 12) {
-            // one 12-step block where no skip falls inside, else three four-value calls
-            float o[12];
-            if (fs_rl_next12<NSKIP>(st, o)) {
-#pragma unroll
-                for (int k = 0; k < 12; k++) c[k % K] = o[k];
-            } else {
 #pragma unroll 1
-                for (int q = 0; q < 3; q++) {
-                    float o0, o1, o2, o3;
-                    fs_rl_next4<NSKIP>(st, o0, o1, o2, o3);
+        for (int q = 0; q < K / 4; q++) {
+            float o0, o1, o2, o3;
+            fs_rl_next4<NSKIP>(st, o0, o1, o2, o3);
 #pragma unroll
-                    for (int k = 0; k < K - 4; k++) c[k] = c[k + 4];
-                    c[K - 4] = o0; c[K - 3] = o1; c[K - 2] = o2; c[K - 1] = o3;
-                }
-            }
-        } else {
-#pragma unroll 1
-            for (int q = 0; q < K / 4; q++) {
-                float o0, o1, o2, o3;
-                fs_rl_next4<NSKIP>(st, o0, o1, o2, o3);
-#pragma unroll
-                for (int k = 0; k < K - 4; k++) c[k] = c[k + 4];
-                c[K - 4] = o0; c[K - 3] = o1; c[K - 2] = o2; c[K - 1] = o3;
-            }
+            for (int k = 0; k < K - 4; k++) c[k] = c[k + 4];
+            c[K - 4] = o0; c[K - 3] = o1; c[K - 2] = o2; c[K - 1] = o3;
         }
         switch (rem) {
         case 0:

@@ -101,13 +101,15 @@ def test_gradients_match_oracle():
     loss_ref, g_ref = mlp_oracle.loss_and_grad(p, x, z, dof, 1.0 / B)
     g = tg.cpu().numpy().astype(np.float64)
     assert abs(float(tl.item()) - loss_ref) < 1e-3 * abs(loss_ref) + 1e-3
-    off = 0
+    off, rels = 0, {}
     for name, n in (("W1", 2048), ("b1", 128), ("W2", 16384), ("b2", 128), ("W3", 16384), ("b3", 128),
                     ("W4", 2048), ("b4", 16)):
         a, b = g[off:off + n], g_ref[off:off + n]
-        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
-        assert rel < 2e-2, (name, rel)
+        rels[name] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12))
         off += n
+    print("\ngradient relative errors (norm of difference / norm):", {k: f"{v:.2e}" for k, v in rels.items()})
+    for name, rel in rels.items():
+        assert rel < 2e-2, (name, rel)
 
 
 def _ho_kernel(learned, N=64, S=3, walkers=2048, beta=8.0, op_runs=20, msteps=2, seed=11):
