@@ -130,10 +130,12 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
 #pragma unroll
                         for (int d = 0; d < DOF; d++) {
                             const float u = fs_xs_float(g), v = fs_xs_float(g);
-                            float rz = 0.f;
-                            if (v != 0.f)
-                                rz = __fmul_rn(__fmul_rn(sig, sqrtf(__fmul_rn(-2.f, __logf(v)))),
-                                               __sinf(__fmul_rn(6.28318548f, u)));
+                            // evaluated for every degree of freedom and replaced by 0 where
+                            // v == 0 (kernel.c:349-353): no branch, so the compiler
+                            // interleaves the degrees of freedom
+                            float rz = __fmul_rn(__fmul_rn(sig, sqrtf(__fmul_rn(-2.f, __logf(v)))),
+                                                 __sinf(__fmul_rn(6.28318548f, u)));
+                            rz = v != 0.f ? rz : 0.f;
                             FSB_AT(P, d, m) = __fadd_rn(__fmul_rn(0.5f, __fadd_rn(FSB_AT(P, d, l), FSB_AT(P, d, r))), rz);
                         }
                     }
