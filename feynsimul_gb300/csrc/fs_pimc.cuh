@@ -500,6 +500,19 @@ __device__ __forceinline__ void fs_flag_nonfinite(int *status, int walker)
     atomicCAS(status + 1, 0, walker + 1);
 }
 
+// Per-launch segment offsets (RANLUX, parallel-path mode): the walker's offset stream feeds
+// only the bisection's segment offsets there (kernel.c:715-718), one draw per Metropolis
+// step, independent of the path.  So one lane draws the launch's FS_OPRUNS * FS_MSTEPS
+// offsets up front into shared memory (one byte each, segments of at most 256 slices), and
+// the steps read them: the same draws in the same order, and the generator's code for that
+// stream stays out of the move loop.
+#define FS_NSTEPS_LAUNCH (FS_OPRUNS * FS_MSTEPS)
+#if FS_RANLUX && FS_PARALLEL && FS_BISECT && FS_SEG <= 256 && FS_NSTEPS_LAUNCH <= 256
+#define FS_OFF_PRE 1
+#else
+#define FS_OFF_PRE 0
+#endif
+
 #ifndef FS_RNG_ONLY
 #if FS_MINB > 0
 #define FS_LAUNCH_BOUNDS __launch_bounds__(FS_BLOCK, FS_MINB)
@@ -511,7 +524,11 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     extern __shared__ __align__(16) unsigned char fs_smem[];
 #if FS_RANLUX
     __shared__ FsIStream s_istream[FS_WPB];
+#if FS_OFF_PRE
+    __shared__ unsigned char s_offs[FS_WPB][FS_NSTEPS_LAUNCH];
+#else
     __shared__ fs_u32 s_off[FS_WPB];
+#endif
 #endif
 #if FS_GLOBAL
     FT *s_v = (FT *)fs_smem;                                     // [WPB][VSTRIDE] (FS_VCACHE)
@@ -586,6 +603,10 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             fs_rl_load(is.st, a.gtab + (size_t)w * 28);
 #endif
             is.count = 0u;
+#if FS_OFF_PRE
+#pragma unroll 1
+            for (int k = 0; k < FS_NSTEPS_LAUNCH; k++) s_offs[wl][k] = (unsigned char)fs_offset(is, FS_SEG);
+#endif
         }
         FS_WSYNC();
 #else
@@ -671,9 +692,13 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #endif
 #if FS_BISECT
 #if FS_RANLUX
+#if FS_OFF_PRE
+                const fs_u32 off = s_offs[wl][run * FS_MSTEPS + step];
+#else
                 if (mover && t == 0) s_off[wl] = fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N);
                 FS_WSYNC();
                 const fs_u32 off = s_off[wl];
+#endif
 #else
                 const fs_u32 off = mover ? fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N) : 0u;
 #endif
