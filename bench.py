@@ -233,7 +233,7 @@ def oracle_cpu_rate(sysm, ka, extra, seconds=10.0, walkers=None):
     seg = 2 ** ka["S"]
     sweeps = runs * msteps
     nodes = W * (ka["N"] // seg) * (seg - 1) * sweeps
-    return {"value": nodes / dt, "unit": "node-updates/s", "cores": cores, "kind": "port",
+    return {"value": nodes / dt, "unit": "node-updates/s", "cores": cores, "kind": "port", "seconds": dt,
             "sample": f"{W} walkers x {sweeps} sweeps of the same system, one measurement every {msteps} "
                       f"sweep(s) ({nodes} node updates, {dt:.1f} s), oracle C restatement, OpenMP over walkers"}
 
@@ -758,15 +758,18 @@ def main():
         for _ in range(args.steps):
             cb = oracle_cpu_rate(sysm, ka, extra, seconds=max(1.0, 60.0 / max(1, args.steps)))
             vals.append(cb["value"])
+            t_all.append(cb["seconds"])
         v = float(np.median(vals))
         out = {"impl": "reference", "metric": "path-node updates/s (plain Metropolis-bisection sampler)",
                "value": v, "unit": "node-updates/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": 1e3 * float(np.mean(t_all)),
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                "data": "synthetic, seeded", "config": bench_config(workload, ka),
                "cpu_baseline": dict(cb, value=v),
                "e2e": {"value": v, "unit": "node-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                "note": "the reference's OpenCL kernels need an OpenCL CPU platform, which is absent; this "
-                       "times the oracle's C restatement of the reference sweep on every host thread"}
+                       "times the oracle's C restatement of the reference sweep on every host thread; a step "
+                       "is a bounded sample of the workload (ms_per_step is its timed part)"}
         print(json.dumps(out))
         return
 
