@@ -287,7 +287,7 @@ def alg_ops_per_node(config, ka):
 
 # DRAM bytes per fs_metropolis launch from one ncu capture of the default workload
 # (dram__bytes_read.sum + dram__bytes_write.sum; profiles/fs_metropolis_he3_lm2m2_ranlux.md)
-TRAFFIC_PER_LAUNCH = {"he3": 225.9e6}
+TRAFFIC_PER_LAUNCH = {"he3": 226.9e6}
 
 
 def roofline_for(config, ka, node_rate, clk, default_workload=True):

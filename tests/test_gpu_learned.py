@@ -108,8 +108,10 @@ def test_gradients_match_oracle():
         rels[name] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12))
         off += n
     print("\ngradient relative errors (norm of difference / norm):", {k: f"{v:.2e}" for k, v in rels.items()})
+    # the oracle rounds to BF16 at the kernel's points, so only the FP32 accumulation order
+    # and the rare BF16 rounding it flips differ: measured 2e-5 .. 2.5e-4 on GB300
     for name, rel in rels.items():
-        assert rel < 2e-2, (name, rel)
+        assert rel < 2e-3, (name, rel)
 
 
 def _ho_kernel(learned, N=64, S=3, walkers=2048, beta=8.0, op_runs=20, msteps=2, seed=11):
