@@ -81,6 +81,8 @@ def workload_overrides(args):
         o["op_runs"] = args.op_runs
     if args.msteps:
         o["msteps"] = args.msteps
+    if args.S:
+        o["S"] = args.S
     return o
 
 
@@ -522,6 +524,8 @@ def precision_bench(args):
         kw["msteps"] = args.msteps
     if args.minb > 0:
         kw["min_blocks"] = args.minb
+    if args.S:
+        kw["S"] = args.S
     import torch
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()        # sampled over the whole study: both arms' timed launches are inside
@@ -692,7 +696,7 @@ def run_gb300(args, rank, world):
 
     # ---- roofline: the sweep is bound by instruction issue (see roofline_for) ----
     roof = roofline_for(args.config, ka, value / world, clk,
-                        default_workload=not (args.walkers or args.op_runs or args.msteps))
+                        default_workload=not (args.walkers or args.op_runs or args.msteps or args.S))
 
     result = {
         "metric": "path-node updates/s (plain Metropolis-bisection sampler)",
@@ -732,6 +736,7 @@ def main():
     ap.add_argument("--walkers", type=int, default=0, help="override the walker count (small cases)")
     ap.add_argument("--op-runs", type=int, default=0, help="override operatorRuns per launch")
     ap.add_argument("--msteps", type=int, default=0, help="override metroStepsPerOperatorRun")
+    ap.add_argument("--S", type=int, default=0, help="override the bisection level")
     ap.add_argument("--wpb", type=int, default=0, help="walkers per thread block (0 = automatic)")
     ap.add_argument("--minb", type=int, default=-1, help="thread blocks per SM to compile for (-1 = tuned default)")
     ap.add_argument("--chunks", type=int, default=0,
