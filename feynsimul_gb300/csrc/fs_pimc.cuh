@@ -489,6 +489,47 @@ __device__ __forceinline__ void fs_kahan(float &s, float &c, float x)
     s = t;
 }
 
+// 16-byte path staging: FS_VEC values of one degree of freedom at slices s .. s + FS_VEC - 1
+// (s a multiple of FS_VEC) are consecutive in global memory and, when 2^S >= FS_VEC, in the
+// padded shared layout.  Every walker's block starts at a multiple of N values, and the
+// paths array is allocated 256-byte aligned, so the 16-byte global accesses are aligned.
+#if FS_DOUBLE
+typedef double2 FsVec;
+#define FS_VEC_N 2
+#else
+typedef float4 FsVec;
+#define FS_VEC_N 4
+#endif
+#if !FS_GLOBAL && FS_N % FS_VEC_N == 0 && (1 << FS_S) >= FS_VEC_N
+#define FS_VEC FS_VEC_N
+#else
+#define FS_VEC 1
+#endif
+__device__ __forceinline__ void fs_vec_scatter(FT *d, const FsVec v)
+{
+#if FS_DOUBLE
+    d[0] = v.x; d[1] = v.y;
+#else
+    d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+#endif
+}
+__device__ __forceinline__ FsVec fs_vec_gather(const FT *d)
+{
+#if FS_DOUBLE
+    return make_double2(d[0], d[1]);
+#else
+    return make_float4(d[0], d[1], d[2], d[3]);
+#endif
+}
+__device__ __forceinline__ bool fs_vec_finite(const FsVec v)
+{
+#if FS_DOUBLE
+    return isfinite(v.x) && isfinite(v.y);
+#else
+    return isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w);
+#endif
+}
+
 // Status word: a path value that is not finite (NaN or infinity) at the end of a launch.
 // Every path value passes through the launch's path-out copy (or, for global paths, the
 // owner's final check), so one compare per value per launch finds any walker whose
@@ -555,11 +596,25 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #if !FS_GLOBAL
         const size_t base = (size_t)w0 * FS_DOF * FS_N;
         const int count = n_here * FS_DOF * FS_N;
+#if FS_VEC > 1
+        // 16-byte loads of FS_VEC consecutive slices; they lie in one 2^S block of the padded
+        // layout, so their shared-memory words are consecutive too
+        const FsVec *src = (const FsVec *)(a.paths + base);
+        for (int i4 = tid_b; i4 < count / FS_VEC; i4 += FS_BLOCK) {
+            const int i = i4 * FS_VEC;
+            const int wi = i / (FS_DOF * FS_N), r = i - wi * (FS_DOF * FS_N);
+            const int d = r / FS_N, sl = r - d * FS_N;
+            FT *dst = &FS_AT(s_path + wi * FS_WSTRIDE, d, sl);
+            const FsVec v = src[i4];
+            fs_vec_scatter(dst, v);
+        }
+#else
         for (int i = tid_b; i < count; i += FS_BLOCK) {
             const int wi = i / (FS_DOF * FS_N), r = i - wi * (FS_DOF * FS_N);
             const int d = r / FS_N, sl = r - d * FS_N;
             FS_AT(s_path + wi * FS_WSTRIDE, d, sl) = a.paths[base + i];
         }
+#endif
 #endif
 #if FS_NHIST > 0
         for (int i = tid_b; i < FS_HBINS; i += FS_BLOCK) s_hist[i] = 0u;
@@ -1046,6 +1101,17 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #if !FS_GLOBAL
         const size_t base = (size_t)w0 * FS_DOF * FS_N;
         const int count = n_here * FS_DOF * FS_N;
+#if FS_VEC > 1
+        FsVec *dstv = (FsVec *)(a.paths + base);
+        for (int i4 = tid_b; i4 < count / FS_VEC; i4 += FS_BLOCK) {
+            const int i = i4 * FS_VEC;
+            const int wi = i / (FS_DOF * FS_N), r = i - wi * (FS_DOF * FS_N);
+            const int d = r / FS_N, sl = r - d * FS_N;
+            const FsVec v = fs_vec_gather(&FS_AT(s_path + wi * FS_WSTRIDE, d, sl));
+            dstv[i4] = v;
+            if (!fs_vec_finite(v)) fs_flag_nonfinite(a.status, w0 + wi);
+        }
+#else
         for (int i = tid_b; i < count; i += FS_BLOCK) {
             const int wi = i / (FS_DOF * FS_N), r = i - wi * (FS_DOF * FS_N);
             const int d = r / FS_N, sl = r - d * FS_N;
@@ -1053,6 +1119,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             a.paths[base + i] = v;
             if (!isfinite(v)) fs_flag_nonfinite(a.status, w0 + wi);
         }
+#endif
 #endif
 #if FS_NHIST > 0
         for (int i = tid_b; i < FS_HBINS; i += FS_BLOCK)

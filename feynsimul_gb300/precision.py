@@ -51,9 +51,9 @@ def _kernel(sysm, walkers, N, S, op_runs, msteps, double, accumulation, seed, fa
     return PIMCKernel(ka)
 
 
-def precision_study(n_atoms=10, N=1024, walkers=2 ** 20, T=1.0, S=3, op_runs=2, msteps=2, launches=8,
+def precision_study(n_atoms=10, N=1024, walkers=2 ** 20, T=1.0, S=2, op_runs=2, msteps=2, launches=8,
                     fp64_walkers=2 ** 14, n_templates=256, seed=2024, fast_math=True, lags=(0, 1, 2, 4, 8),
-                    burn_in=2, log=None, min_blocks=0):
+                    burn_in=2, log=None, min_blocks=2):
     """Run the study (``burn_in`` launches of both arms before the measured ones, after
     which the accumulators are zeroed); returns a dict of results (JSON-serialisable)."""
     from .physical_systems.lm2m2 import Lm2m2Cluster
