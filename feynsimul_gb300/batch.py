@@ -42,8 +42,10 @@ def ragged_workload(seed=0, n_systems=64, n_range=(3, 10), N_choices=(128, 256, 
 def choose_S(N, tpw_target, block, dof=None, smem_budget=200 * 1024):
     """Bisection level of one system: N / 2^S = tpw_target segment threads per walker, except
     where a walker's path fills most of a tile's shared memory (large clusters): then the
-    walker gets up to the whole CTA (segments of at least 8 slices), so the tile does not
-    leave most of its warps idle."""
+    walker gets up to the whole CTA (segments of at least 4 slices), so the tile does not
+    leave warps idle at its barriers.  With segments of at least 8 slices, five of the
+    standard workload's system types left 64-256 of a 512-thread CTA idle: 5.76e9 against
+    6.44e9 node updates/s with 4."""
     S = int(np.log2(N)) - int(np.log2(tpw_target))
     S = max(1, min(S, 10, int(np.log2(N))))
     if dof is not None:
@@ -51,7 +53,7 @@ def choose_S(N, tpw_target, block, dof=None, smem_budget=200 * 1024):
         wpb_max = max(1, smem_budget // walker_bytes)
         if wpb_max * (N >> S) < block and N >= 8:
             tpw = 1 << int(np.log2(max(1, block // wpb_max)))
-            tpw = min(tpw, N // 8)
+            tpw = min(tpw, N // 4)
             S = min(S, max(1, int(np.log2(N // tpw))))
     while (N >> S) > block:
         S += 1
@@ -152,7 +154,7 @@ class BatchSampler:
 
 
 # bumped when the batch kernel or its launch-shape rules change, so cached tunings expire
-_TUNING_VERSION = 3
+_TUNING_VERSION = 4
 
 
 def _signature(workload, op_runs, msteps):
