@@ -315,6 +315,7 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << (c.enable_parallelize_path ? 1 : 0) << "\n#define FS_RANLUX " << (c.enable_ranlux ? 1 : 0)
       << "\n#define FS_NSKIP " << (c.enable_ranlux ? nskip_for(c.luxury_factor + 1) : 0)
       << "\n#define FS_COMPAT " << (c.compat ? 1 : 0) << "\n#define FS_ACCUM " << c.accum
+      << "\n#define FS_COR_PART " << c.cor_partials
       << "\n#define FS_FAST " << (c.fast_math ? 1 : 0) << "\n#define FS_NOPS " << h.ops.size()
       << "\n#define FS_NCOR " << h.cors.size() << "\n#define FS_OPRUNS " << c.operator_runs
       << "\n#define FS_MSTEPS " << c.metro_steps_per_operator_run << "\n#define FS_EPS "
@@ -558,6 +559,8 @@ static int validate(const fs_config &c, int nops, int ncor, int nhist)
     if (nhist > 0 && (c.hist_bins < 1 || c.hist_bins > 16384 || !(c.hist_hi > c.hist_lo)))
         return fail(nullptr, FS_ERR_CONFIG, "histogram needs 1..16384 bins and hist_lo < hist_hi");
     if (c.accum < 0 || c.accum > 3) return fail(nullptr, FS_ERR_CONFIG, "accum must be 0..3");
+    if (c.cor_partials != FS_COR_PARTIALS_FP32 && c.cor_partials != FS_COR_PARTIALS_FLOAT_FLOAT)
+        return fail(nullptr, FS_ERR_CONFIG, "cor_partials must be 0 (FP32) or 1 (float-float)");
     if (nops < 0 || ncor < 0 || nops > 64 || ncor > 16)
         return fail(nullptr, FS_ERR_CONFIG, "at most 64 operators and 16 correlators");
     if (c.walkers_per_block < 0) return fail(nullptr, FS_ERR_CONFIG, "walkers_per_block must be >= 0");

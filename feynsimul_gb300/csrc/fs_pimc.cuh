@@ -40,18 +40,28 @@
 #endif
 #define FS_COR_REGS (FS_ACCUM != 3 && FS_LPT * FS_NCOR <= 16)
 #define FS_CSTEP (FS_N % 4 == 0 ? 4 : 1)  // FP64 correlator: partial sums over s1 mod 4
-// Correlator FP64 sums of FP32 builds (FP64, Kahan and study modes): float-float per
-// measurement (fs_ff_add), then one FP64 add per lag; the study's FP32 and Kahan columns sum
-// the same products in slice order.  FS_COR_ILV (set by the host, which sizes shared memory
-// for it): a thread owning at most 4 lags sums them in one pass over the slice values, which
-// are stored twice in a row (FS_CSTRIDE = 2N words per correlator) so that slice s1 + tau is
-// read without a wrap.
-#define FS_COR_FF (FS_ACCUM != 0 && !FS_DOUBLE)
+// Correlator FP64 sums of FP32 builds (FP64, Kahan and study modes): one measurement's
+// products of a lag are summed in FP32, then added to the lag's FP64 running sum.  The FP32
+// partial (FS_COR_PART, fs_config.cor_partials) is either four fused multiply-add chains
+// over the slices s1 mod 4, added pairwise (FS_COR_FMA; 0, the default), or the rounded
+// products in float-float (FS_COR_FF, fs_ff_add; 1, and always in the study mode, whose FP32
+// and Kahan columns sum the same products in slice order).  The FMA partial of an N-slice
+// lag sum is within gamma(N/4 + 2) * sum_s |x_s x_(s+tau)| <= gamma(N/4 + 2) * C(0) of the
+// exact sum (gamma(n) = n u / (1 - n u), u = 2^-24; sum_s |x_s x_(s+tau)| <= sum_s x_s^2 by
+// Cauchy-Schwarz).  FS_COR_ILV (set by the host, which sizes shared memory for it): a thread
+// owning at most 4 lags sums them in one pass over the slice values, which are stored twice
+// in a row (FS_CSTRIDE = 2N words per correlator) so that slice s1 + tau is read without a
+// wrap.
+#ifndef FS_COR_PART
+#define FS_COR_PART 0
+#endif
+#define FS_COR_FMA ((FS_ACCUM == 1 || FS_ACCUM == 2) && !FS_DOUBLE && FS_COR_PART == 0)
+#define FS_COR_FF (FS_ACCUM != 0 && !FS_DOUBLE && !FS_COR_FMA)
 #ifndef FS_COR_ILV
 #define FS_COR_ILV 0
 #endif
-#if FS_COR_ILV && !(FS_COR_FF && FS_LPT <= 4 && FS_LPT * FS_CTPW <= FS_N)
-#error "FS_COR_ILV needs float-float correlator sums and at most 4 lags per thread"
+#if FS_COR_ILV && !((FS_COR_FF || FS_COR_FMA) && FS_LPT <= 4 && FS_LPT * FS_CTPW <= FS_N)
+#error "FS_COR_ILV needs FP32 correlator partials and at most 4 lags per thread"
 #endif
 #define FS_CSTRIDE (FS_COR_ILV ? 2 * FS_N : FS_N)
 #ifndef FS_CWSTRIDE
@@ -879,6 +889,49 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                 // against 1.80-1.87e9 node updates/s at 8).  Lags past N/2 (when
                 // FS_CTPW does not divide N/2) are summed and dropped; s1 + tau < N + LPT * CTPW
                 // <= 2N stays inside the doubled slice values.
+#if FS_COR_FMA
+                {
+                    // four FMA chains per lag (slices s1 mod 4); the slice values s1..s1+3
+                    // in one 16-byte load (Cc is 16-byte aligned: the host pads every
+                    // stride to 64 bytes), shared by all lags of the thread
+                    float pa[FS_LPT][4];
+#pragma unroll
+                    for (int j = 0; j < FS_LPT; j++)
+#pragma unroll
+                        for (int k = 0; k < 4; k++) pa[j][k] = 0.0f;
+#if FS_N % 4 == 0
+#pragma unroll 2
+                    for (int s1 = 0; s1 < FS_N; s1 += 4) {
+                        const float4 c4 = *reinterpret_cast<const float4 *>(Cc + s1);
+#pragma unroll
+                        for (int j = 0; j < FS_LPT; j++) {
+                            const float *cj = Cc + s1 + lt + j * FS_CTPW;
+                            pa[j][0] = __fmaf_rn(c4.x, cj[0], pa[j][0]);
+                            pa[j][1] = __fmaf_rn(c4.y, cj[1], pa[j][1]);
+                            pa[j][2] = __fmaf_rn(c4.z, cj[2], pa[j][2]);
+                            pa[j][3] = __fmaf_rn(c4.w, cj[3], pa[j][3]);
+                        }
+                    }
+#else
+#pragma unroll
+                    for (int s1 = 0; s1 < FS_N; s1++)
+#pragma unroll
+                        for (int j = 0; j < FS_LPT; j++)
+                            pa[j][s1 & 3] = __fmaf_rn(Cc[s1], Cc[s1 + lt + j * FS_CTPW], pa[j][s1 & 3]);
+#endif
+#pragma unroll
+                    for (int j = 0; j < FS_LPT; j++) {
+                        const double m =
+                            fs_f2d(__fadd_rn(__fadd_rn(pa[j][0], pa[j][1]), __fadd_rn(pa[j][2], pa[j][3])));
+#if FS_COR_REGS
+                        cacc[c][j] = __dadd_rn(cacc[c][j], m);
+#else
+                        const int tau = lt + j * FS_CTPW;
+                        if (tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = __dadd_rn(g_cor[c * FS_HALF_N + tau], m);
+#endif
+                    }
+                }
+#else
                 {
                     float fs[FS_LPT], fe[FS_LPT];
 #if FS_ACCUM == 3
@@ -930,6 +983,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #endif
                     }
                 }
+#endif  // FS_COR_FMA
 #else
 #if FS_COR_REGS
 #pragma unroll
@@ -944,7 +998,23 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #else
                     FsCorAcc acc = g_cor[c * FS_HALF_N + tau];
 #endif
-#if FS_COR_FF
+#if FS_COR_FMA
+                    {
+                        float p[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#if FS_N % 4 == 0
+#pragma unroll 2
+                        for (int s1 = 0; s1 < FS_N; s1 += 4)
+#pragma unroll
+                            for (int k = 0; k < 4; k++)
+                                p[k] = __fmaf_rn(Cc[s1 + k], Cc[(s1 + k + tau) & (FS_N - 1)], p[k]);
+#else
+#pragma unroll
+                        for (int s1 = 0; s1 < FS_N; s1++)
+                            p[s1 & 3] = __fmaf_rn(Cc[s1], Cc[(s1 + tau) & (FS_N - 1)], p[s1 & 3]);
+#endif
+                        acc = __dadd_rn(acc, fs_f2d(__fadd_rn(__fadd_rn(p[0], p[1]), __fadd_rn(p[2], p[3]))));
+                    }
+#elif FS_COR_FF
                     {
                         float fs = 0.0f, fe = 0.0f;
 #pragma unroll 4

@@ -1,0 +1,61 @@
+"""Correlator partial sums on the GPU: the default FP32 partials (four fused multiply-add
+chains per lag and measurement) against float-float partials of the same trajectory.
+
+Both add one FP64 term per lag and measurement to the running sums, and the moves do not
+depend on the accumulation, so the paths are bit-identical and the running sums differ only
+by the partials' rounding.  Bound per measurement, with u = 2^-24 and
+gamma(n) = n u / (1 - n u): the FMA partial is within gamma(N/4 + 2) * sum_s |a_s a_(s+tau)|
+of the exact sum, and the float-float sum of the rounded products within
+(u + 2^-44) * sum_s |a_s a_(s+tau)|; by Cauchy-Schwarz sum_s |a_s a_(s+tau)| <= sum_s a_s^2,
+the lag-0 term.  Summed over measurements: |fp32 - float-float| <= (gamma + 2u) * C(0)."""
+import types
+
+import numpy as np
+import pytest
+
+from gpu_util import engine, require_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def _kernel(partials, parallel, N, S, W=256):
+    kernel, kernel_args = engine()
+    sysm = types.SimpleNamespace(DOF=1, potential="0.5 * x1 * x1", userCode="")
+    ka = kernel_args.KernelArgs(
+        system=sysm, nbrOfWalkers=W, N=N, beta=10.0, S=S, enableOperator=True, enableCorrelator=True,
+        enableBisection=True, enablePathShift=False, enableSingleNodeMove=False, enableBins=False,
+        nbrOfWalkersPerWorkGroup=1, enableParallelizePath=parallel, enableGlobalPath=False,
+        enableGlobalOldPath=False, operators=("x1 * x1",), correlators=("x1", "x1 * x1 - 0.5"),
+        operatorRuns=6, metroStepsPerOperatorRun=2, correlatorPartials=partials, seed=11)
+    return kernel.PIMCKernel(ka)
+
+
+@pytest.mark.parametrize("parallel,N,S", [
+    (True, 128, 3),    # 16 segment threads + 48 helper threads, one lag each
+    (True, 64, 2),     # 16 segment threads + 16 helpers, one lag each
+    (True, 256, 2),    # 64 segment threads, two lags each, no helpers
+    (False, 64, 2),    # one thread per walker: all 32 lags in one loop, sums in device memory
+], ids=["helpers4", "helpers2", "two_lags", "walker_mode"])
+def test_fp32_partials_within_bound_of_float_float(parallel, N, S):
+    require_gpu()
+    W = 256
+    kf, kx = _kernel("fp32", parallel, N, S, W), _kernel("float-float", parallel, N, S, W)
+    p0 = (np.random.RandomState(5).randn(W, N) * 0.7).astype(np.float32)
+    for k in (kf, kx):
+        k.setPaths(p0)
+    for _ in range(3):
+        kf.run()
+        kx.run()
+    assert np.array_equal(kf.getPaths(), kx.getPaths())
+    a = kf._raw_correlator().reshape(W, 2, N // 2)
+    b = kx._raw_correlator().reshape(W, 2, N // 2)
+    u = 2.0 ** -24
+    n = N // 4 + 2
+    bound = (n * u / (1 - n * u) + 2 * u) * b[:, :, :1]
+    err = np.abs(a - b)
+    assert np.all(err <= bound), (err / bound).max()
+    assert np.all(b[:, :, 0] > 0)
+    # the bound resolves the values: far below the statistical spread of the lag sums
+    assert bound.max() < 1e-4 * b[:, :, 0].std()
+    kf.close()
+    kx.close()

@@ -5,8 +5,9 @@
 * the FP64-everywhere sweep of a 10-atom LM2M2 cluster agrees with the CPU oracle's FP64
   build (same generator streams; CUDA's and libm's exp/log/sin may differ in the last
   ulp, hence rtol 1e-9 on paths);
-* study accumulation: its FP64 column equals the FP64 mode's sums bit for bit, the
-  device-side correlator moments equal the host reduction;
+* study accumulation: its FP64 column equals the FP64 mode's sums (with float-float
+  correlator partials) bit for bit, the device-side correlator moments equal the host
+  reduction;
 * a small precision study: FP32-path results within statistical error of FP64-everywhere.
 """
 import numpy as np
@@ -29,7 +30,7 @@ def _cluster(n):
 
 
 def _kernel(sysm, walkers, N, S, global_path, double=False, accumulation="fp64", fast=False, op_runs=2,
-            msteps=2, ranlux=False, seed=3):
+            msteps=2, ranlux=False, seed=3, partials="fp32"):
     kernel, kernel_args = engine()
     from feynsimul_gb300.precision import hyperradius2
     ka = kernel_args.KernelArgs(
@@ -39,7 +40,8 @@ def _kernel(sysm, walkers, N, S, global_path, double=False, accumulation="fp64",
         enableGlobalPath=global_path, enableGlobalOldPath=False, enableDouble=double,
         enableRanlux=ranlux, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
         operators=(sysm.energyOp,), correlators=(hyperradius2(sysm.DOF),), operatorRuns=op_runs,
-        metroStepsPerOperatorRun=msteps, accumulation=accumulation, fastMath=fast, seed=seed)
+        metroStepsPerOperatorRun=msteps, accumulation=accumulation, fastMath=fast, seed=seed,
+        correlatorPartials=partials)
     k = kernel.PIMCKernel(ka)
     if ranlux:
         k.initRanlux()
@@ -104,7 +106,8 @@ def test_study_columns_and_device_moments():
     # IEEE builds: with FMA contraction allowed, two differently generated modules may
     # round the operator expression differently
     ks = _kernel(sysm, W, N, S, True, accumulation="study", fast=False)
-    kd = _kernel(sysm, W, N, S, True, accumulation="fp64", fast=False)
+    # the study's FP64 column sums each measurement in float-float
+    kd = _kernel(sysm, W, N, S, True, accumulation="fp64", fast=False, partials="float-float")
     p0 = sysm.initial_paths(W, N, np.random.RandomState(4)).astype(np.float32)
     for k in (ks, kd):
         k.setPaths(p0)
