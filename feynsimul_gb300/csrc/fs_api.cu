@@ -67,6 +67,7 @@ struct fs_handle {
     // launch geometry
     int tpw = 1, seg = 1, wpb = 1, block = 1, grid = 1;
     int cor_ilv = 0;  // correlator lags summed in one slice pass over a doubled slice buffer
+    int pipe = 0;     // correlator helpers one measurement behind the movers (FS_PIPE)
     int mx = 1;       // thread groups per CTA: 1 moving + mx - 1 summing correlator lags (FS_MX)
     long long cwstride = 0;  // per-walker correlator buffer in shared memory, elements
     int resident_per_sm = 0;  // resident CTAs per SM of the sweep kernel (fs_run_host), 0 = not yet queried
@@ -324,7 +325,7 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n#define FS_GLOBAL " << (c.global_path ? 1 : 0)
       << "\n#define FS_VCACHE " << (h.vstride ? 1 : 0) << "\n#define FS_VSTRIDE " << h.vstride
       << "\n#define FS_COR_ILV " << h.cor_ilv << "\n#define FS_CWSTRIDE " << h.cwstride << "\n#define FS_MX "
-      << h.mx << "\n";
+      << h.mx << "\n#define FS_PIPE " << h.pipe << "\n";
     {
         const int mv = c.moves ? c.moves : FS_MOVE_BISECTION;
         const double nb = (double)c.n_slices / c.beta;
@@ -639,17 +640,29 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
         // Correlator helpers: a walker of at most 32 segment threads gets extra threads for
         // the lag sums, up to 64 lag threads per walker (FS_MX in fs_pimc.cuh).  They need
         // every CTA full (the walker count a multiple of the walkers per CTA, chosen below).
+        // Where the movers of a CTA fill whole warps (walker count and walkers per CTA
+        // multiples of 32 / threads per walker) the helpers are pipelined (FS_PIPE): they
+        // alone sum the lags, one measurement behind the movers.
         if (!h->cors.empty() && c.enable_parallelize_path && !c.global_path && !c.learned && h->tpw <= 32) {
             const int lag_threads = std::min(c.n_slices / 2, 64);
-            if (lag_threads > h->tpw) h->mx = lag_threads / h->tpw;
-            if (c.walkers_per_block > 0 && c.n_walkers % c.walkers_per_block) h->mx = 1;
+            if (lag_threads > h->tpw) {
+                const int wpw = 32 / h->tpw;
+                const int groups = lag_threads / h->tpw + 1;
+                const int wpb_min = c.walkers_per_block > 0 ? c.walkers_per_block : wpw;
+                const bool whole_warps = c.n_walkers % wpw == 0 && wpb_min % wpw == 0 &&
+                                         (long long)wpb_min * h->tpw * groups <= 512;
+                h->pipe = whole_warps ? 1 : 0;
+                h->mx = lag_threads / h->tpw + h->pipe;
+            }
+            if (c.walkers_per_block > 0 && c.n_walkers % c.walkers_per_block) h->mx = 1, h->pipe = 0;
         }
-        const long long lpt = (c.n_slices / 2 + (long long)h->tpw * h->mx - 1) / ((long long)h->tpw * h->mx);
+        const long long lag_tpw = (long long)h->tpw * (h->mx - h->pipe);
+        const long long lpt = (c.n_slices / 2 + lag_tpw - 1) / lag_tpw;
         h->cor_ilv = (c.accum != 0 && !c.enable_double && lpt <= 4) ? 1 : 0;
         // per-walker stride an odd multiple of 64 bytes: two walkers sharing a warp read
         // opposite bank halves
         const long long q = 64 / (long long)h->ft;
-        long long cw = (long long)h->cors.size() * c.n_slices * (h->cor_ilv ? 2 : 1);
+        long long cw = (long long)h->cors.size() * c.n_slices * (h->cor_ilv ? 2 : 1) * (1 + h->pipe);
         if (cw) {
             cw = ((cw + q - 1) / q) * q;
             if ((cw / q) % 2 == 0) cw += q;
@@ -679,9 +692,12 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     if (c.walkers_per_block > 0) {
         h->wpb = c.walkers_per_block;
     } else if (h->mx > 1) {
-        // CTAs of about 128 threads (moving and summing), every CTA full
-        h->wpb = std::max(1, 128 / (h->tpw * h->mx));
-        while (h->wpb > 1 && (c.n_walkers % h->wpb || per_walker * h->wpb + hist_bytes > 100 * 1024)) h->wpb--;
+        // CTAs of about 128 threads (moving and summing), every CTA full; pipelined: the
+        // movers in whole warps
+        const int step = h->pipe ? 32 / h->tpw : 1;
+        h->wpb = std::max(step, 128 / (h->tpw * h->mx) / step * step);
+        while (h->wpb > step && (c.n_walkers % h->wpb || per_walker * h->wpb + hist_bytes > 100 * 1024))
+            h->wpb -= step;
     } else if (h->tpw > 32) {
         h->wpb = 1;
     } else {

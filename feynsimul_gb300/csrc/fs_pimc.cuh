@@ -28,15 +28,25 @@
 // moves and the per-slice measurement; every group sums correlator lags, so a walker's N/2
 // lags spread over FS_TPW x FS_MX threads instead of its FS_TPW segment threads.  Each lag is
 // still summed by one thread in slice order, so the sums are the same bit for bit.
+// FS_PIPE (the host sets it where the movers fill whole warps): only the helper groups sum
+// lags, and they do it for measurement m while the movers sweep towards measurement m + 1;
+// the slice values are double-buffered, one CTA barrier per measurement hands a buffer over,
+// and the movers sync among themselves on a named barrier the helpers never wait on.
 #ifndef FS_MX
 #define FS_MX 1
 #endif
+#ifndef FS_PIPE
+#define FS_PIPE 0
+#endif
 #define FS_MBLOCK (FS_WPB * FS_TPW)          // threads that run the moves
 #define FS_BLOCK (FS_MBLOCK * FS_MX)
-#define FS_CTPW (FS_TPW * FS_MX)             // correlator threads per walker
+#define FS_CTPW (FS_TPW * (FS_MX - FS_PIPE))  // correlator threads per walker
 #define FS_LPT ((FS_HALF_N + FS_CTPW - 1) / FS_CTPW)  // correlator lags owned per thread
 #if FS_MX > 1 && (!FS_PARALLEL || FS_TPW > 32 || FS_GLOBAL || FS_NCOR == 0 || FS_NWALKERS % FS_WPB != 0)
 #error "correlator helpers need parallel-path walkers of at most 32 threads in shared memory, correlators, and full CTAs"
+#endif
+#if FS_PIPE && (FS_MX < 2 || FS_MBLOCK % 32 != 0 || FS_LEARNED)
+#error "pipelined correlator helpers need helper groups and whole warps of movers"
 #endif
 #define FS_COR_REGS (FS_ACCUM != 3 && FS_LPT * FS_NCOR <= 16)
 #define FS_CSTEP (FS_N % 4 == 0 ? 4 : 1)  // FP64 correlator: partial sums over s1 mod 4
@@ -67,7 +77,7 @@
 #ifndef FS_CWSTRIDE
 #define FS_CWSTRIDE (FS_NCOR * FS_CSTRIDE)  // per-walker correlator buffer (the host pads it)
 #endif
-#if FS_CWSTRIDE < FS_NCOR * FS_CSTRIDE
+#if FS_CWSTRIDE < (1 + FS_PIPE) * FS_NCOR * FS_CSTRIDE
 #error "per-walker correlator buffer smaller than its slice values"
 #endif
 
@@ -595,7 +605,9 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     const int wl = (tid_b - grp * FS_MBLOCK) / FS_TPW;
     const int t = tid_b % FS_TPW;
     const bool mover = FS_MX == 1 || grp == 0;
-    const int lt = grp * FS_TPW + t;               // this thread's lags: lt + j * FS_CTPW
+    // this thread's lags: lt + j * FS_CTPW; with FS_PIPE only the helpers own lags
+    const bool lagger = !FS_PIPE || !mover;
+    const int lt = (grp - FS_PIPE) * FS_TPW + t;
     const int w0 = (blockIdx.x + a.block_offset) * FS_WPB;
     const int w = w0 + wl;
     const int n_here = min(FS_WPB, FS_NWALKERS - w0);
@@ -633,7 +645,14 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     __syncthreads();
 
     if (active) {
-#if FS_TPW <= 32 && FS_MX == 1
+#if FS_PIPE
+        // the movers' own barrier (whole warps; the helpers never wait on it)
+#if FS_MBLOCK == 32
+#define FS_WSYNC() do { if (mover) __syncwarp(); } while (0)
+#else
+#define FS_WSYNC() do { if (mover) asm volatile("bar.sync 1, %0;" ::"n"(FS_MBLOCK) : "memory"); } while (0)
+#endif
+#elif FS_TPW <= 32 && FS_MX == 1
         const unsigned lane = threadIdx.x & 31u;
         const unsigned wmask = FS_TPW == 32 ? 0xFFFFFFFFu
                                             : (((1u << FS_TPW) - 1u) << (lane / FS_TPW * FS_TPW));
@@ -705,7 +724,8 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #endif
 #if FS_NCOR > 0
         FsCorAcc *g_cor = (FsCorAcc *)a.cor_means + (size_t)w * FS_NCOR * FS_HALF_N;
-        FT *C = s_cor + wl * FS_CWSTRIDE;
+        FT *const C0 = s_cor + wl * FS_CWSTRIDE;
+        FT *C = C0;  // the slice values of the current measurement
 #if FS_COR_REGS
         FsCorAcc cacc[FS_NCOR][FS_LPT];
 #pragma unroll
@@ -713,7 +733,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #pragma unroll
             for (int j = 0; j < FS_LPT; j++) {
                 const int tau = lt + j * FS_CTPW;
-                cacc[c][j] = tau < FS_HALF_N ? g_cor[c * FS_HALF_N + tau] : (FsCorAcc)0;
+                cacc[c][j] = lagger && tau < FS_HALF_N ? g_cor[c * FS_HALF_N + tau] : (FsCorAcc)0;
             }
 #endif
 #endif
@@ -732,154 +752,13 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         FS_WSYNC();
 #endif
 
-        // ---- sweeps (kernel.c:628-799) ----
-#pragma unroll 1
-        for (int run = 0; run < FS_OPRUNS; run++) {
-#pragma unroll 1
-            for (int step = 0; step < FS_MSTEPS; step++) {
-#if !FS_PARALLEL && (FS_PATH_SHIFT || FS_SNM)
-                {
-                    // walker-mode moves ahead of the bisection (kernel.c:640-705).  The
-                    // reference's step counter i*mSteps + j restarts every launch; the fixed
-                    // mode continues it across launches.
-#if FS_COMPAT
-                    const unsigned long long k = (unsigned long long)run * FS_MSTEPS + step;
-#else
-                    const unsigned long long k = a.step_base + (unsigned long long)run * FS_MSTEPS + step;
-#endif
-#if FS_PATH_SHIFT
-                    n_acc += (fs_u32)fs_path_shift_move(P, k, is, fs, a.shift_old + (size_t)w * FS_N);
-#endif
-#if FS_SNM
-                    n_acc += (fs_u32)fs_single_node_move(P, k, fs);
-#endif
-                }
-#endif
-#if FS_BISECT
-#if FS_RANLUX
-#if FS_OFF_PRE
-                const fs_u32 off = s_offs[wl][run * FS_MSTEPS + step];
-#else
-                if (mover && t == 0) s_off[wl] = fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N);
-                FS_WSYNC();
-                const fs_u32 off = s_off[wl];
-#endif
-#else
-                const fs_u32 off = mover ? fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N) : 0u;
-#endif
-#if FS_PARALLEL
-                const fs_u32 start = (off + (fs_u32)(FS_SEG * t)) & (FS_N - 1);
-#else
-                const fs_u32 start = off;
-#endif
-#if FS_LEARNED
-                // level-1 proposal from the segment's endpoints (warp-wide network evaluation)
-                FT lmu[FS_DOF], lsd[FS_DOF];
-                {
-                    float feat[FS_MLP_IN], out[FS_MLP_OUT];
-#pragma unroll
-                    for (int k = 0; k < FS_MLP_IN; k++) feat[k] = 0.f;
-                    const fs_u32 e1 = (start + FS_SEG) & (FS_N - 1);
-#pragma unroll
-                    for (int d = 0; d < FS_DOF; d++) {
-                        const FT x0 = FS_AT(P, d, start), x1 = FS_AT(P, d, e1);
-                        feat[d] = 0.5f * (x0 + x1) * a.mlp_inv_scale;
-                        feat[FS_DOF + d] = 0.5f * (x1 - x0) * a.mlp_inv_scale;
-                    }
-                    fs_mlp_eval_warp(a.mlp_frag, a.mlp_bias, feat, out);
-                    const FT s1 = sigma[1];
-#pragma unroll
-                    for (int d = 0; d < FS_DOF; d++) {
-                        const FT mid = 0.5f * (FS_AT(P, d, start) + FS_AT(P, d, e1));
-                        float o = out[d], sv = 4.f * tanhf(0.25f * out[FS_DOF + d]);
-                        if (!(fabsf(o) < 64.f) || !(fabsf(sv) <= 4.f)) {  // non-finite: free proposal
-                            o = 0.f;
-                            sv = 0.f;
-                        }
-                        lmu[d] = mid + s1 * o;
-                        lsd[d] = s1 * __expf(0.5f * sv);
-                    }
-                }
-                n_acc += (fs_u32)fs_bisect(P, Vc, start, fs, sigma, lmu, lsd);
-#else
-                if (mover) n_acc += (fs_u32)fs_bisect(P, Vc, start, fs, sigma, nullptr, nullptr);
-#endif
-#endif  // FS_BISECT
-                FS_WSYNC();
-            }
-            // ---- measurement (kernel.c:734-797) ----
-#if FS_PARALLEL
-            const int s_lo = t * FS_SEG, s_hi = (t + 1) * FS_SEG;
-#else
-            const int s_lo = 0, s_hi = FS_N;
-#endif
-#pragma unroll 1
-            for (int s = s_lo; s < (mover ? s_hi : s_lo); s++) {
-#if FS_NOPS > 0
-                FT ov[FS_NOPS];
-                fs_ops(FS_ARGS_AT(P, s), ov);
-#pragma unroll
-                for (int i = 0; i < FS_NOPS; i++) {
-#if FS_ACCUM == 0
-                    opr[i] = FS_ADD(opr[i], ov[i]);
-#elif FS_ACCUM == 1
-                    opd[i] = __dadd_rn(opd[i], fs_f2d(ov[i]));
-#elif FS_ACCUM == 2
-                    fs_kahan(opks[i], opkc[i], (float)ov[i]);
-#else
-                    opf[i] = __fadd_rn(opf[i], (float)ov[i]);
-                    fs_kahan(opks[i], opkc[i], (float)ov[i]);
-                    opd[i] = __dadd_rn(opd[i], fs_f2d(ov[i]));
-#endif
-                }
-#endif
-#if FS_BINS
-                {
-                    int ok = 1, inc = 1, bi = 0;
-#pragma unroll
-                    for (int d = 0; d < FS_DOF; d++) {
-                        const FT x = FS_AT(P, d, s);
-                        if (x < (FT)FS_XMIN || x >= (FT)FS_XMAX) ok = 0;
-                        bi += (int)((fs_u32)FS_MUL(FS_SUB(x, (FT)FS_XMIN), (FT)FS_INVBIN)) * inc;
-                        inc *= FS_BINRES;
-                    }
-                    if (ok) atomicAdd(a.bins + bi, 1u);
-                }
-#endif
-#if FS_NHIST > 0
-                {
-                    FT hv[FS_NHIST];
-                    fs_hist(FS_ARGS_AT(P, s), hv);
-#pragma unroll
-                    for (int h = 0; h < FS_NHIST; h++) {
-                        const FT x = hv[h];
-                        if (x >= (FT)FS_HLO && x < (FT)FS_HHI) {
-                            const int b = (int)FS_MUL(FS_SUB(x, (FT)FS_HLO), (FT)FS_HINVW);
-                            if (b >= 0 && b < FS_HBINS) atomicAdd(s_hist + b, 1u);
-                        }
-                    }
-                }
-#endif
 #if FS_NCOR > 0
-                {
-                    FT cv[FS_NCOR];
-                    fs_cors(FS_ARGS_AT(P, s), cv);
-#pragma unroll
-                    for (int c = 0; c < FS_NCOR; c++) {
-                        C[c * FS_CSTRIDE + s] = cv[c];
-#if FS_COR_ILV
-                        C[c * FS_CSTRIDE + s + FS_N] = cv[c];
-#endif
-                    }
-                }
-#endif
-            }
-#if FS_NCOR > 0
-            FS_WSYNC();
-            // lags tau = lt + j * FS_CTPW owned by this thread
+        // one measurement's lag sums of the slice values in Cm, added to the lags this thread
+        // owns: tau = lt + j * FS_CTPW
+        auto fs_cor_lags = [&](const FT *Cm) {
 #pragma unroll
             for (int c = 0; c < FS_NCOR; c++) {
-                const FT *Cc = C + c * FS_CSTRIDE;
+                const FT *Cc = Cm + c * FS_CSTRIDE;
 #if FS_COR_ILV
                 // every lag this thread owns in one pass over the slices: 2 x FS_LPT independent
                 // float-float chains, and Cc[s1] loaded once for all lags.  Unrolled by 8 (HO,
@@ -1099,8 +978,174 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                 }
 #endif
             }
+        };
+#endif
+
+        // ---- sweeps (kernel.c:628-799) ----
+#if FS_PIPE
+        if (!mover) {
+            // correlator helpers: the lag sums of measurement run while the movers sweep
+            // towards the next one (the slice values are double-buffered in C0)
+#pragma unroll 1
+            for (int run = 0; run < FS_OPRUNS; run++) {
+                __syncthreads();
+                fs_cor_lags(C0 + (run & 1) * (FS_NCOR * FS_CSTRIDE));
+            }
+        } else
+#endif
+        {
+#pragma unroll 1
+        for (int run = 0; run < FS_OPRUNS; run++) {
+#pragma unroll 1
+            for (int step = 0; step < FS_MSTEPS; step++) {
+#if !FS_PARALLEL && (FS_PATH_SHIFT || FS_SNM)
+                {
+                    // walker-mode moves ahead of the bisection (kernel.c:640-705).  The
+                    // reference's step counter i*mSteps + j restarts every launch; the fixed
+                    // mode continues it across launches.
+#if FS_COMPAT
+                    const unsigned long long k = (unsigned long long)run * FS_MSTEPS + step;
+#else
+                    const unsigned long long k = a.step_base + (unsigned long long)run * FS_MSTEPS + step;
+#endif
+#if FS_PATH_SHIFT
+                    n_acc += (fs_u32)fs_path_shift_move(P, k, is, fs, a.shift_old + (size_t)w * FS_N);
+#endif
+#if FS_SNM
+                    n_acc += (fs_u32)fs_single_node_move(P, k, fs);
+#endif
+                }
+#endif
+#if FS_BISECT
+#if FS_RANLUX
+#if FS_OFF_PRE
+                const fs_u32 off = s_offs[wl][run * FS_MSTEPS + step];
+#else
+                if (mover && t == 0) s_off[wl] = fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N);
+                FS_WSYNC();
+                const fs_u32 off = s_off[wl];
+#endif
+#else
+                const fs_u32 off = mover ? fs_offset(is, FS_PARALLEL ? FS_SEG : FS_N) : 0u;
+#endif
+#if FS_PARALLEL
+                const fs_u32 start = (off + (fs_u32)(FS_SEG * t)) & (FS_N - 1);
+#else
+                const fs_u32 start = off;
+#endif
+#if FS_LEARNED
+                // level-1 proposal from the segment's endpoints (warp-wide network evaluation)
+                FT lmu[FS_DOF], lsd[FS_DOF];
+                {
+                    float feat[FS_MLP_IN], out[FS_MLP_OUT];
+#pragma unroll
+                    for (int k = 0; k < FS_MLP_IN; k++) feat[k] = 0.f;
+                    const fs_u32 e1 = (start + FS_SEG) & (FS_N - 1);
+#pragma unroll
+                    for (int d = 0; d < FS_DOF; d++) {
+                        const FT x0 = FS_AT(P, d, start), x1 = FS_AT(P, d, e1);
+                        feat[d] = 0.5f * (x0 + x1) * a.mlp_inv_scale;
+                        feat[FS_DOF + d] = 0.5f * (x1 - x0) * a.mlp_inv_scale;
+                    }
+                    fs_mlp_eval_warp(a.mlp_frag, a.mlp_bias, feat, out);
+                    const FT s1 = sigma[1];
+#pragma unroll
+                    for (int d = 0; d < FS_DOF; d++) {
+                        const FT mid = 0.5f * (FS_AT(P, d, start) + FS_AT(P, d, e1));
+                        float o = out[d], sv = 4.f * tanhf(0.25f * out[FS_DOF + d]);
+                        if (!(fabsf(o) < 64.f) || !(fabsf(sv) <= 4.f)) {  // non-finite: free proposal
+                            o = 0.f;
+                            sv = 0.f;
+                        }
+                        lmu[d] = mid + s1 * o;
+                        lsd[d] = s1 * __expf(0.5f * sv);
+                    }
+                }
+                n_acc += (fs_u32)fs_bisect(P, Vc, start, fs, sigma, lmu, lsd);
+#else
+                if (mover) n_acc += (fs_u32)fs_bisect(P, Vc, start, fs, sigma, nullptr, nullptr);
+#endif
+#endif  // FS_BISECT
+                FS_WSYNC();
+            }
+            // ---- measurement (kernel.c:734-797) ----
+#if FS_PARALLEL
+            const int s_lo = t * FS_SEG, s_hi = (t + 1) * FS_SEG;
+#else
+            const int s_lo = 0, s_hi = FS_N;
+#endif
+#pragma unroll 1
+            for (int s = s_lo; s < (mover ? s_hi : s_lo); s++) {
+#if FS_NOPS > 0
+                FT ov[FS_NOPS];
+                fs_ops(FS_ARGS_AT(P, s), ov);
+#pragma unroll
+                for (int i = 0; i < FS_NOPS; i++) {
+#if FS_ACCUM == 0
+                    opr[i] = FS_ADD(opr[i], ov[i]);
+#elif FS_ACCUM == 1
+                    opd[i] = __dadd_rn(opd[i], fs_f2d(ov[i]));
+#elif FS_ACCUM == 2
+                    fs_kahan(opks[i], opkc[i], (float)ov[i]);
+#else
+                    opf[i] = __fadd_rn(opf[i], (float)ov[i]);
+                    fs_kahan(opks[i], opkc[i], (float)ov[i]);
+                    opd[i] = __dadd_rn(opd[i], fs_f2d(ov[i]));
+#endif
+                }
+#endif
+#if FS_BINS
+                {
+                    int ok = 1, inc = 1, bi = 0;
+#pragma unroll
+                    for (int d = 0; d < FS_DOF; d++) {
+                        const FT x = FS_AT(P, d, s);
+                        if (x < (FT)FS_XMIN || x >= (FT)FS_XMAX) ok = 0;
+                        bi += (int)((fs_u32)FS_MUL(FS_SUB(x, (FT)FS_XMIN), (FT)FS_INVBIN)) * inc;
+                        inc *= FS_BINRES;
+                    }
+                    if (ok) atomicAdd(a.bins + bi, 1u);
+                }
+#endif
+#if FS_NHIST > 0
+                {
+                    FT hv[FS_NHIST];
+                    fs_hist(FS_ARGS_AT(P, s), hv);
+#pragma unroll
+                    for (int h = 0; h < FS_NHIST; h++) {
+                        const FT x = hv[h];
+                        if (x >= (FT)FS_HLO && x < (FT)FS_HHI) {
+                            const int b = (int)FS_MUL(FS_SUB(x, (FT)FS_HLO), (FT)FS_HINVW);
+                            if (b >= 0 && b < FS_HBINS) atomicAdd(s_hist + b, 1u);
+                        }
+                    }
+                }
+#endif
+#if FS_NCOR > 0
+                {
+                    FT cv[FS_NCOR];
+                    fs_cors(FS_ARGS_AT(P, s), cv);
+#pragma unroll
+                    for (int c = 0; c < FS_NCOR; c++) {
+                        C[c * FS_CSTRIDE + s] = cv[c];
+#if FS_COR_ILV
+                        C[c * FS_CSTRIDE + s + FS_N] = cv[c];
+#endif
+                    }
+                }
+#endif
+            }
+#if FS_NCOR > 0
+#if FS_PIPE
+            __syncthreads();  // the measurement's slice values go to the helper threads
+            C = C == C0 ? C0 + FS_NCOR * FS_CSTRIDE : C0;
+#else
+            FS_WSYNC();
+            fs_cor_lags(C);
+#endif
 #endif
             FS_WSYNC();
+        }
         }
 
         // ---- epilogue (kernel.c:801-836) ----
@@ -1128,7 +1173,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #pragma unroll
             for (int j = 0; j < FS_LPT; j++) {
                 const int tau = lt + j * FS_CTPW;
-                if (tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = cacc[c][j];
+                if (lagger && tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = cacc[c][j];
             }
 #endif
 #if FS_GLOBAL

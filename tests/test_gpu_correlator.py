@@ -7,7 +7,10 @@ by the partials' rounding.  Bound per measurement, with u = 2^-24 and
 gamma(n) = n u / (1 - n u): the FMA partial is within gamma(N/4 + 2) * sum_s |a_s a_(s+tau)|
 of the exact sum, and the float-float sum of the rounded products within
 (u + 2^-44) * sum_s |a_s a_(s+tau)|; by Cauchy-Schwarz sum_s |a_s a_(s+tau)| <= sum_s a_s^2,
-the lag-0 term.  Summed over measurements: |fp32 - float-float| <= (gamma + 2u) * C(0)."""
+the lag-0 term.  Summed over measurements: |fp32 - float-float| <= (gamma + 2u) * C(0).
+
+Also: the pipelined correlator helpers (lag sums one measurement behind the moves) give the
+same bits as helpers that wait for the moves."""
 import types
 
 import numpy as np
@@ -18,7 +21,7 @@ from gpu_util import engine, require_gpu
 pytestmark = pytest.mark.gpu
 
 
-def _kernel(partials, parallel, N, S, W=256):
+def _kernel(partials, parallel, N, S, W=256, wpb=0):
     kernel, kernel_args = engine()
     sysm = types.SimpleNamespace(DOF=1, potential="0.5 * x1 * x1", userCode="")
     ka = kernel_args.KernelArgs(
@@ -26,7 +29,8 @@ def _kernel(partials, parallel, N, S, W=256):
         enableBisection=True, enablePathShift=False, enableSingleNodeMove=False, enableBins=False,
         nbrOfWalkersPerWorkGroup=1, enableParallelizePath=parallel, enableGlobalPath=False,
         enableGlobalOldPath=False, operators=("x1 * x1",), correlators=("x1", "x1 * x1 - 0.5"),
-        operatorRuns=6, metroStepsPerOperatorRun=2, correlatorPartials=partials, seed=11)
+        operatorRuns=6, metroStepsPerOperatorRun=2, correlatorPartials=partials, walkersPerBlock=wpb,
+        seed=11)
     return kernel.PIMCKernel(ka)
 
 
@@ -59,3 +63,28 @@ def test_fp32_partials_within_bound_of_float_float(parallel, N, S):
     assert bound.max() < 1e-4 * b[:, :, 0].std()
     kf.close()
     kx.close()
+
+
+@pytest.mark.parametrize("partials", ["fp32", "float-float"])
+def test_pipelined_helpers_bit_identical(partials):
+    """The launch shapes of one HO run (N = 128, S = 3: 16 segment threads per walker):
+    2 walkers per CTA pipeline 64 helper threads per walker one measurement behind the
+    movers; 1 walker per CTA leaves the movers in half warps, so every thread of 4 groups
+    sums lags after the moves.  Each lag is summed by one thread in the same order either
+    way, so paths, operators, accepts and correlator sums are bit-identical."""
+    require_gpu()
+    W, N = 256, 128
+    kp, kh = _kernel(partials, True, N, 3, W, wpb=2), _kernel(partials, True, N, 3, W, wpb=1)
+    assert kp._info.block_threads == 2 * 16 * 5 and kh._info.block_threads == 16 * 4
+    p0 = (np.random.RandomState(6).randn(W, N) * 0.7).astype(np.float32)
+    for k in (kp, kh):
+        k.setPaths(p0)
+    for _ in range(3):
+        kp.run()
+        kh.run()
+    assert np.array_equal(kp.getPaths(), kh.getPaths())
+    assert np.array_equal(kp._raw_operators(), kh._raw_operators())
+    assert np.array_equal(kp.getAccepts(), kh.getAccepts())
+    assert np.array_equal(kp._raw_correlator(), kh._raw_correlator())
+    kp.close()
+    kh.close()
