@@ -42,7 +42,7 @@ EXPORTS = (
 )
 
 FS_MOVE_BISECTION, FS_MOVE_PATH_SHIFT, FS_MOVE_SINGLE_NODE = 1, 2, 4
-FS_COR_PARTIALS_FP32, FS_COR_PARTIALS_FLOAT_FLOAT = 0, 1
+FS_PARTIALS_FP32, FS_PARTIALS_EXACT = 0, 1
 
 
 class FsConfig(ctypes.Structure):
@@ -60,7 +60,7 @@ class FsConfig(ctypes.Structure):
         ("walkers_per_block", ctypes.c_int32), ("min_blocks_per_sm", ctypes.c_int32),
         ("learned", ctypes.c_int32), ("global_path", ctypes.c_int32), ("potential_cache", ctypes.c_int32),
         ("moves", ctypes.c_int32), ("alpha", ctypes.c_double), ("ps_alpha", ctypes.c_double),
-        ("cor_partials", ctypes.c_int32),
+        ("partials", ctypes.c_int32),
     ]
 
 

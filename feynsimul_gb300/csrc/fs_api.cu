@@ -68,6 +68,7 @@ struct fs_handle {
     int tpw = 1, seg = 1, wpb = 1, block = 1, grid = 1;
     int cor_ilv = 0;  // correlator lags summed in one slice pass over a doubled slice buffer
     int pipe = 0;     // correlator helpers one measurement behind the movers (FS_PIPE)
+    long long snstride = 0;  // FS_PIPE: one path snapshot in shared memory, elements
     int mx = 1;       // thread groups per CTA: 1 moving + mx - 1 summing correlator lags (FS_MX)
     long long cwstride = 0;  // per-walker correlator buffer in shared memory, elements
     int resident_per_sm = 0;  // resident CTAs per SM of the sweep kernel (fs_run_host), 0 = not yet queried
@@ -316,7 +317,7 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << (c.enable_parallelize_path ? 1 : 0) << "\n#define FS_RANLUX " << (c.enable_ranlux ? 1 : 0)
       << "\n#define FS_NSKIP " << (c.enable_ranlux ? nskip_for(c.luxury_factor + 1) : 0)
       << "\n#define FS_COMPAT " << (c.compat ? 1 : 0) << "\n#define FS_ACCUM " << c.accum
-      << "\n#define FS_COR_PART " << c.cor_partials
+      << "\n#define FS_PARTIALS " << c.partials
       << "\n#define FS_FAST " << (c.fast_math ? 1 : 0) << "\n#define FS_NOPS " << h.ops.size()
       << "\n#define FS_NCOR " << h.cors.size() << "\n#define FS_OPRUNS " << c.operator_runs
       << "\n#define FS_MSTEPS " << c.metro_steps_per_operator_run << "\n#define FS_EPS "
@@ -325,7 +326,7 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n#define FS_GLOBAL " << (c.global_path ? 1 : 0)
       << "\n#define FS_VCACHE " << (h.vstride ? 1 : 0) << "\n#define FS_VSTRIDE " << h.vstride
       << "\n#define FS_COR_ILV " << h.cor_ilv << "\n#define FS_CWSTRIDE " << h.cwstride << "\n#define FS_MX "
-      << h.mx << "\n#define FS_PIPE " << h.pipe << "\n";
+      << h.mx << "\n#define FS_PIPE " << h.pipe << "\n#define FS_SNSTRIDE " << h.snstride << "\n";
     {
         const int mv = c.moves ? c.moves : FS_MOVE_BISECTION;
         const double nb = (double)c.n_slices / c.beta;
@@ -560,8 +561,8 @@ static int validate(const fs_config &c, int nops, int ncor, int nhist)
     if (nhist > 0 && (c.hist_bins < 1 || c.hist_bins > 16384 || !(c.hist_hi > c.hist_lo)))
         return fail(nullptr, FS_ERR_CONFIG, "histogram needs 1..16384 bins and hist_lo < hist_hi");
     if (c.accum < 0 || c.accum > 3) return fail(nullptr, FS_ERR_CONFIG, "accum must be 0..3");
-    if (c.cor_partials != FS_COR_PARTIALS_FP32 && c.cor_partials != FS_COR_PARTIALS_FLOAT_FLOAT)
-        return fail(nullptr, FS_ERR_CONFIG, "cor_partials must be 0 (FP32) or 1 (float-float)");
+    if (c.partials != FS_PARTIALS_FP32 && c.partials != FS_PARTIALS_EXACT)
+        return fail(nullptr, FS_ERR_CONFIG, "partials must be 0 (FP32) or 1 (exact)");
     if (nops < 0 || ncor < 0 || nops > 64 || ncor > 16)
         return fail(nullptr, FS_ERR_CONFIG, "at most 64 operators and 16 correlators");
     if (c.walkers_per_block < 0) return fail(nullptr, FS_ERR_CONFIG, "walkers_per_block must be >= 0");
@@ -634,35 +635,50 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     h->n_threads = (long long)c.n_walkers * h->tpw;
     h->ft = c.enable_double ? 8 : 4;
     {
-        // float-float correlator sums (every mode but the reference's FP32 order, FP32 builds)
-        // with at most 4 lags per thread run every lag in one pass over the slice values,
-        // stored twice in a row so that slice s1 + tau needs no wrap
+        // FP32-partial correlator sums (every mode but the reference's FP32 order, FP32
+        // builds) with at most 4 lags per thread run every lag in one pass over the slice
+        // values, stored twice in a row so that slice s1 + tau needs no wrap.
         // Correlator helpers: a walker of at most 32 segment threads gets extra threads for
         // the lag sums, up to 64 lag threads per walker (FS_MX in fs_pimc.cuh).  They need
         // every CTA full (the walker count a multiple of the walkers per CTA, chosen below).
         // Where the movers of a CTA fill whole warps (walker count and walkers per CTA
-        // multiples of 32 / threads per walker) the helpers are pipelined (FS_PIPE): they
-        // alone sum the lags, one measurement behind the movers.
+        // multiples of 32 / threads per walker) the helpers are pipelined (FS_PIPE): the
+        // movers copy their slices to a double-buffered path snapshot, and the helpers alone
+        // evaluate the operators and correlator values on it and sum the lags, one
+        // measurement behind the moves.
+        // The pipelined helpers give each pair of threads 4 consecutive lags (N/4 lag threads
+        // per walker, in pairs of one walker: an even number of segment threads) and sum
+        // FP32 partials over the doubled slice values.
         if (!h->cors.empty() && c.enable_parallelize_path && !c.global_path && !c.learned && h->tpw <= 32) {
             const int lag_threads = std::min(c.n_slices / 2, 64);
-            if (lag_threads > h->tpw) {
-                const int wpw = 32 / h->tpw;
-                const int groups = lag_threads / h->tpw + 1;
-                const int wpb_min = c.walkers_per_block > 0 ? c.walkers_per_block : wpw;
-                const bool whole_warps = c.n_walkers % wpw == 0 && wpb_min % wpw == 0 &&
-                                         (long long)wpb_min * h->tpw * groups <= 512;
-                h->pipe = whole_warps ? 1 : 0;
-                h->mx = lag_threads / h->tpw + h->pipe;
+            const int wpw = 32 / h->tpw;
+            const int wpb_min = c.walkers_per_block > 0 ? c.walkers_per_block : wpw;
+            const int groups = (c.n_slices / 4 + h->tpw - 1) / h->tpw;
+            const bool fma_partials = (c.accum == FS_ACCUM_FP64 || c.accum == FS_ACCUM_KAHAN) &&
+                                      !c.enable_double && c.partials == FS_PARTIALS_FP32;
+            if (fma_partials && c.n_slices % 8 == 0 && c.n_slices >= 16 && h->tpw >= 2 && c.n_walkers % wpw == 0 &&
+                wpb_min % wpw == 0 && c.n_walkers % wpb_min == 0 &&
+                (long long)wpb_min * h->tpw * (1 + groups) <= 512) {
+                h->pipe = 1;
+                h->mx = 1 + groups;
+            } else if (lag_threads > h->tpw) {
+                h->mx = lag_threads / h->tpw;
             }
             if (c.walkers_per_block > 0 && c.n_walkers % c.walkers_per_block) h->mx = 1, h->pipe = 0;
         }
         const long long lag_tpw = (long long)h->tpw * (h->mx - h->pipe);
-        const long long lpt = (c.n_slices / 2 + lag_tpw - 1) / lag_tpw;
+        const long long lpt = h->pipe ? 4 : (c.n_slices / 2 + lag_tpw - 1) / lag_tpw;
         h->cor_ilv = (c.accum != 0 && !c.enable_double && lpt <= 4) ? 1 : 0;
         // per-walker stride an odd multiple of 64 bytes: two walkers sharing a warp read
         // opposite bank halves
         const long long q = 64 / (long long)h->ft;
-        long long cw = (long long)h->cors.size() * c.n_slices * (h->cor_ilv ? 2 : 1) * (1 + h->pipe);
+        long long cw = (long long)h->cors.size() * c.n_slices * (h->cor_ilv ? 2 : 1);
+        if (h->pipe) {
+            // two path snapshots in the padded slice layout, 16-word multiples (FS_SNSTRIDE)
+            const long long dstr = c.n_slices + (c.n_slices >> c.bisection_level);
+            h->snstride = ((c.dof * dstr + 15) / 16) * 16;
+            cw += 2 * h->snstride;
+        }
         if (cw) {
             cw = ((cw + q - 1) / q) * q;
             if ((cw / q) % 2 == 0) cw += q;
@@ -694,8 +710,10 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     } else if (h->mx > 1) {
         // CTAs of about 128 threads (moving and summing), every CTA full; pipelined: the
         // movers in whole warps
+        // pipelined: the movers in whole warps, as few walkers per CTA as that allows (the
+        // CTAs spread evenly over the SMs)
         const int step = h->pipe ? 32 / h->tpw : 1;
-        h->wpb = std::max(step, 128 / (h->tpw * h->mx) / step * step);
+        h->wpb = h->pipe ? step : std::max(1, 128 / (h->tpw * h->mx));
         while (h->wpb > step && (c.n_walkers % h->wpb || per_walker * h->wpb + hist_bytes > 100 * 1024))
             h->wpb -= step;
     } else if (h->tpw > 32) {

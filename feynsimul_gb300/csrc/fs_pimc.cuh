@@ -28,31 +28,44 @@
 // moves and the per-slice measurement; every group sums correlator lags, so a walker's N/2
 // lags spread over FS_TPW x FS_MX threads instead of its FS_TPW segment threads.  Each lag is
 // still summed by one thread in slice order, so the sums are the same bit for bit.
-// FS_PIPE (the host sets it where the movers fill whole warps): only the helper groups sum
-// lags, and they do it for measurement m while the movers sweep towards measurement m + 1;
-// the slice values are double-buffered, one CTA barrier per measurement hands a buffer over,
-// and the movers sync among themselves on a named barrier the helpers never wait on.
+// FS_PIPE (the host sets it where the movers fill whole warps): the movers measure by
+// copying their slices into a double-buffered path snapshot (FS_SNSTRIDE words each, the
+// padded slice layout); the helper groups evaluate the operators (group 1, for the segment
+// of the same index, in the mover's order) and the correlator values on the snapshot and
+// sum the lags, for measurement m while the movers sweep towards measurement m + 1.  One CTA
+// barrier per measurement hands a snapshot over; the movers sync among themselves on named
+// barrier 1 and the helpers on named barrier 2.  Every sum is formed by one thread in the
+// same order as without the pipeline, so the results are the same bit for bit.
 #ifndef FS_MX
 #define FS_MX 1
 #endif
 #ifndef FS_PIPE
 #define FS_PIPE 0
 #endif
+#ifndef FS_SNSTRIDE
+#define FS_SNSTRIDE 0
+#endif
 #define FS_MBLOCK (FS_WPB * FS_TPW)          // threads that run the moves
 #define FS_BLOCK (FS_MBLOCK * FS_MX)
 #define FS_CTPW (FS_TPW * (FS_MX - FS_PIPE))  // correlator threads per walker
+#if FS_PIPE
+#define FS_LPT 4                             // lags 2 lt .. 2 lt + 3 (even lt)
+#define FS_LAG(j) (2 * lt + (j))
+#else
 #define FS_LPT ((FS_HALF_N + FS_CTPW - 1) / FS_CTPW)  // correlator lags owned per thread
+#define FS_LAG(j) (lt + (j) * FS_CTPW)
+#endif
 #if FS_MX > 1 && (!FS_PARALLEL || FS_TPW > 32 || FS_GLOBAL || FS_NCOR == 0 || FS_NWALKERS % FS_WPB != 0)
 #error "correlator helpers need parallel-path walkers of at most 32 threads in shared memory, correlators, and full CTAs"
 #endif
-#if FS_PIPE && (FS_MX < 2 || FS_MBLOCK % 32 != 0 || FS_LEARNED)
-#error "pipelined correlator helpers need helper groups and whole warps of movers"
+#if FS_PIPE && (FS_MX < 2 || FS_MBLOCK % 32 != 0 || FS_LEARNED || FS_SNSTRIDE < FS_DOF * (FS_N + (FS_N >> FS_S)) || FS_SNSTRIDE % 16 != 0 || FS_N % 8 != 0 || FS_CTPW < FS_N / 4 || FS_TPW % 2 != 0)
+#error "pipelined correlator helpers need helper groups, whole warps of movers and a path snapshot"
 #endif
 #define FS_COR_REGS (FS_ACCUM != 3 && FS_LPT * FS_NCOR <= 16)
 #define FS_CSTEP (FS_N % 4 == 0 ? 4 : 1)  // FP64 correlator: partial sums over s1 mod 4
 // Correlator FP64 sums of FP32 builds (FP64, Kahan and study modes): one measurement's
 // products of a lag are summed in FP32, then added to the lag's FP64 running sum.  The FP32
-// partial (FS_COR_PART, fs_config.cor_partials) is either four fused multiply-add chains
+// partial (FS_PARTIALS, fs_config.partials) is either four fused multiply-add chains
 // over the slices s1 mod 4, added pairwise (FS_COR_FMA; 0, the default), or the rounded
 // products in float-float (FS_COR_FF, fs_ff_add; 1, and always in the study mode, whose FP32
 // and Kahan columns sum the same products in slice order).  The FMA partial of an N-slice
@@ -62,22 +75,30 @@
 // owning at most 4 lags sums them in one pass over the slice values, which are stored twice
 // in a row (FS_CSTRIDE = 2N words per correlator) so that slice s1 + tau is read without a
 // wrap.
-#ifndef FS_COR_PART
-#define FS_COR_PART 0
+#ifndef FS_PARTIALS
+#define FS_PARTIALS 0
 #endif
-#define FS_COR_FMA ((FS_ACCUM == 1 || FS_ACCUM == 2) && !FS_DOUBLE && FS_COR_PART == 0)
+#define FS_COR_FMA ((FS_ACCUM == 1 || FS_ACCUM == 2) && !FS_DOUBLE && FS_PARTIALS == 0)
+// Operator FP64 sums of FP32 builds ("fp64" accumulation, FS_PARTIALS 0, parallel-path
+// mode): a segment thread's 2^S values of one measurement summed in FP32 in slice order,
+// within gamma(2^S) * sum |value| of the exact sum, then one FP64 add (GB300's FP64 pipe is
+// narrow: a chain of FP64 adds per slice made the measurement latency bound)
+#define FS_OP_PART (FS_ACCUM == 1 && !FS_DOUBLE && FS_PARTIALS == 0 && FS_PARALLEL)
 #define FS_COR_FF (FS_ACCUM != 0 && !FS_DOUBLE && !FS_COR_FMA)
 #ifndef FS_COR_ILV
 #define FS_COR_ILV 0
 #endif
-#if FS_COR_ILV && !((FS_COR_FF || FS_COR_FMA) && FS_LPT <= 4 && FS_LPT * FS_CTPW <= FS_N)
+#if FS_COR_ILV && !((FS_COR_FF || FS_COR_FMA) && FS_LPT <= 4 && (FS_PIPE || FS_LPT * FS_CTPW <= FS_N))
 #error "FS_COR_ILV needs FP32 correlator partials and at most 4 lags per thread"
+#endif
+#if FS_PIPE && !(FS_COR_FMA && FS_COR_ILV)
+#error "pipelined correlator helpers sum FP32 partials over doubled slice values"
 #endif
 #define FS_CSTRIDE (FS_COR_ILV ? 2 * FS_N : FS_N)
 #ifndef FS_CWSTRIDE
 #define FS_CWSTRIDE (FS_NCOR * FS_CSTRIDE)  // per-walker correlator buffer (the host pads it)
 #endif
-#if FS_CWSTRIDE < (1 + FS_PIPE) * FS_NCOR * FS_CSTRIDE
+#if FS_CWSTRIDE < 2 * FS_SNSTRIDE + FS_NCOR * FS_CSTRIDE
 #error "per-walker correlator buffer smaller than its slice values"
 #endif
 
@@ -605,9 +626,10 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     const int wl = (tid_b - grp * FS_MBLOCK) / FS_TPW;
     const int t = tid_b % FS_TPW;
     const bool mover = FS_MX == 1 || grp == 0;
-    // this thread's lags: lt + j * FS_CTPW; with FS_PIPE only the helpers own lags
-    const bool lagger = !FS_PIPE || !mover;
+    // this thread's lags FS_LAG(j): lt + j * FS_CTPW; with FS_PIPE the even helper lanes
+    // lt < N/4 own lags 2 lt + j
     const int lt = (grp - FS_PIPE) * FS_TPW + t;
+    const bool lagger = FS_PIPE ? !mover && lt < FS_N / 4 && (lt & 1) == 0 : true;
     const int w0 = (blockIdx.x + a.block_offset) * FS_WPB;
     const int w = w0 + wl;
     const int n_here = min(FS_WPB, FS_NWALKERS - w0);
@@ -716,23 +738,27 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #if FS_NOPS > 0
         FT opr[FS_NOPS];
         double opd[FS_NOPS];
-        float opf[FS_NOPS], opks[FS_NOPS], opkc[FS_NOPS];
+        float opf[FS_NOPS], opks[FS_NOPS], opkc[FS_NOPS], opp[FS_NOPS];
 #pragma unroll
         for (int i = 0; i < FS_NOPS; i++) {
-            opr[i] = (FT)0; opd[i] = 0.0; opf[i] = 0.0f; opks[i] = 0.0f; opkc[i] = 0.0f;
+            opr[i] = (FT)0; opd[i] = 0.0; opf[i] = 0.0f; opks[i] = 0.0f; opkc[i] = 0.0f; opp[i] = 0.0f;
         }
 #endif
 #if FS_NCOR > 0
         FsCorAcc *g_cor = (FsCorAcc *)a.cor_means + (size_t)w * FS_NCOR * FS_HALF_N;
-        FT *const C0 = s_cor + wl * FS_CWSTRIDE;
-        FT *C = C0;  // the slice values of the current measurement
+        // FS_PIPE: two path snapshots ahead of the correlator values
+        FT *const C = s_cor + wl * FS_CWSTRIDE + 2 * FS_SNSTRIDE;  // one measurement's values
+#if FS_PIPE
+        FT *const SN0 = s_cor + wl * FS_CWSTRIDE;
+        FT *SN = SN0;  // the movers' next snapshot
+#endif
 #if FS_COR_REGS
         FsCorAcc cacc[FS_NCOR][FS_LPT];
 #pragma unroll
         for (int c = 0; c < FS_NCOR; c++)
 #pragma unroll
             for (int j = 0; j < FS_LPT; j++) {
-                const int tau = lt + j * FS_CTPW;
+                const int tau = FS_LAG(j);
                 cacc[c][j] = lagger && tau < FS_HALF_N ? g_cor[c * FS_HALF_N + tau] : (FsCorAcc)0;
             }
 #endif
@@ -752,7 +778,53 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         FS_WSYNC();
 #endif
 
+#if FS_NOPS > 0
+        // the operators of slice s of path Q, added to this thread's sums
+        auto fs_op_add = [&](const FT *Q, int s) {
+            FT ov[FS_NOPS];
+            fs_ops(FS_ARGS_AT(Q, s), ov);
+#pragma unroll
+            for (int i = 0; i < FS_NOPS; i++) {
+#if FS_ACCUM == 0
+                opr[i] = FS_ADD(opr[i], ov[i]);
+#elif FS_OP_PART
+                opp[i] = __fadd_rn(opp[i], (float)ov[i]);
+#elif FS_ACCUM == 1
+                opd[i] = __dadd_rn(opd[i], fs_f2d(ov[i]));
+#elif FS_ACCUM == 2
+                fs_kahan(opks[i], opkc[i], (float)ov[i]);
+#else
+                opf[i] = __fadd_rn(opf[i], (float)ov[i]);
+                fs_kahan(opks[i], opkc[i], (float)ov[i]);
+                opd[i] = __dadd_rn(opd[i], fs_f2d(ov[i]));
+#endif
+            }
+        };
+        // end of one measurement's operator values: the FP32 partials into the FP64 sums
+        auto fs_op_flush = [&]() {
+#if FS_OP_PART
+#pragma unroll
+            for (int i = 0; i < FS_NOPS; i++) {
+                opd[i] = __dadd_rn(opd[i], fs_f2d(opp[i]));
+                opp[i] = 0.0f;
+            }
+#endif
+        };
+#endif
 #if FS_NCOR > 0
+        // the correlator values of slice s of path Q into the measurement's buffer C
+        auto fs_cor_put = [&](const FT *Q, int s) {
+            FT cv[FS_NCOR];
+            fs_cors(FS_ARGS_AT(Q, s), cv);
+#pragma unroll
+            for (int c = 0; c < FS_NCOR; c++) {
+                C[c * FS_CSTRIDE + s] = cv[c];
+#if FS_COR_ILV
+                C[c * FS_CSTRIDE + s + FS_N] = cv[c];
+#endif
+            }
+        };
+#if !FS_PIPE
         // one measurement's lag sums of the slice values in Cm, added to the lags this thread
         // owns: tau = lt + j * FS_CTPW
         auto fs_cor_lags = [&](const FT *Cm) {
@@ -979,17 +1051,80 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #endif
             }
         };
+#else
+        // pipelined helpers: a pair of lanes (lt = 2 p + h) sums lags 4 p .. 4 p + 3 of one
+        // measurement, lane h the chains of slices s1 = 2 h, 2 h + 1 (mod 4); the same four
+        // chains per lag in slice order and the same pairwise combination as the lag sums
+        // above, so the same bits: lane h adds its two chains, the even lane adds the odd
+        // lane's pair sum (a shuffle) and owns the FP64 sums.  8-byte loads: the slice pair
+        // s1 + 2h, s1 + 2h + 1 and the window s1 + 4p + 2h .. + 4, the window's upper half
+        // carried to the next step (3 loads per 8 products).  Reads stop at slice
+        // 3N/2 - 1 of the doubled values.  Every helper lane runs it (the shuffles).
+        auto fs_cor_lags4 = [&](const FT *Cm) {
+            const bool on = lt < FS_N / 4;
+            const int p = lt >> 1, h = lt & 1;
+#pragma unroll
+            for (int c = 0; c < FS_NCOR; c++) {
+                float sp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                if (on) {
+                    const float2 *cv2 = reinterpret_cast<const float2 *>(Cm + c * FS_CSTRIDE);
+                    const float2 *wv2 = cv2 + 2 * p + h;
+                    float pa[4][2];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) pa[j][0] = pa[j][1] = 0.0f;
+                    float2 w0 = wv2[0];
+#pragma unroll 4
+                    for (int q = 0; q < FS_N / 4; q++) {
+                        const float2 a2 = cv2[2 * q + h];
+                        const float2 w1 = wv2[2 * q + 1], w2 = wv2[2 * q + 2];
+                        const float wv[5] = {w0.x, w0.y, w1.x, w1.y, w2.x};
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            pa[j][0] = __fmaf_rn(a2.x, wv[j], pa[j][0]);
+                            pa[j][1] = __fmaf_rn(a2.y, wv[j + 1], pa[j][1]);
+                        }
+                        w0 = w2;
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; j++) sp[j] = __fadd_rn(pa[j][0], pa[j][1]);
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const float o = __shfl_down_sync(0xffffffffu, sp[j], 1);
+                    if (lagger) {
+                        const double m = fs_f2d(__fadd_rn(sp[j], o));
+#if FS_COR_REGS
+                        cacc[c][j] = __dadd_rn(cacc[c][j], m);
+#else
+                        g_cor[c * FS_HALF_N + FS_LAG(j)] = __dadd_rn(g_cor[c * FS_HALF_N + FS_LAG(j)], m);
+#endif
+                    }
+                }
+            }
+        };
+#endif
 #endif
 
         // ---- sweeps (kernel.c:628-799) ----
 #if FS_PIPE
         if (!mover) {
-            // correlator helpers: the lag sums of measurement run while the movers sweep
-            // towards the next one (the slice values are double-buffered in C0)
+            // helpers: measurement run on its snapshot while the movers sweep towards the
+            // next one
 #pragma unroll 1
             for (int run = 0; run < FS_OPRUNS; run++) {
                 __syncthreads();
-                fs_cor_lags(C0 + (run & 1) * (FS_NCOR * FS_CSTRIDE));
+                const FT *Q = SN0 + (run & 1) * FS_SNSTRIDE;
+#if FS_NOPS > 0
+                if (grp == 1) {
+#pragma unroll 1
+                    for (int s = t * FS_SEG; s < (t + 1) * FS_SEG; s++) fs_op_add(Q, s);
+                    fs_op_flush();
+                }
+#endif
+#pragma unroll 1
+                for (int s = lt; s < FS_N; s += FS_CTPW) fs_cor_put(Q, s);
+                asm volatile("bar.sync 2, %0;" ::"n"(FS_BLOCK - FS_MBLOCK) : "memory");
+                fs_cor_lags4(C);
             }
         } else
 #endif
@@ -1076,23 +1211,16 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #endif
 #pragma unroll 1
             for (int s = s_lo; s < (mover ? s_hi : s_lo); s++) {
-#if FS_NOPS > 0
-                FT ov[FS_NOPS];
-                fs_ops(FS_ARGS_AT(P, s), ov);
+#if FS_PIPE
 #pragma unroll
-                for (int i = 0; i < FS_NOPS; i++) {
-#if FS_ACCUM == 0
-                    opr[i] = FS_ADD(opr[i], ov[i]);
-#elif FS_ACCUM == 1
-                    opd[i] = __dadd_rn(opd[i], fs_f2d(ov[i]));
-#elif FS_ACCUM == 2
-                    fs_kahan(opks[i], opkc[i], (float)ov[i]);
+                for (int d = 0; d < FS_DOF; d++) FS_AT(SN, d, s) = FS_AT(P, d, s);
 #else
-                    opf[i] = __fadd_rn(opf[i], (float)ov[i]);
-                    fs_kahan(opks[i], opkc[i], (float)ov[i]);
-                    opd[i] = __dadd_rn(opd[i], fs_f2d(ov[i]));
+#if FS_NOPS > 0
+                fs_op_add(P, s);
 #endif
-                }
+#if FS_NCOR > 0
+                fs_cor_put(P, s);
+#endif
 #endif
 #if FS_BINS
                 {
@@ -1121,28 +1249,16 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                     }
                 }
 #endif
-#if FS_NCOR > 0
-                {
-                    FT cv[FS_NCOR];
-                    fs_cors(FS_ARGS_AT(P, s), cv);
-#pragma unroll
-                    for (int c = 0; c < FS_NCOR; c++) {
-                        C[c * FS_CSTRIDE + s] = cv[c];
-#if FS_COR_ILV
-                        C[c * FS_CSTRIDE + s + FS_N] = cv[c];
-#endif
-                    }
-                }
-#endif
             }
-#if FS_NCOR > 0
+#if FS_NOPS > 0 && !FS_PIPE
+            if (mover) fs_op_flush();
+#endif
 #if FS_PIPE
-            __syncthreads();  // the measurement's slice values go to the helper threads
-            C = C == C0 ? C0 + FS_NCOR * FS_CSTRIDE : C0;
-#else
+            __syncthreads();  // the snapshot goes to the helper threads
+            SN = SN == SN0 ? SN0 + FS_SNSTRIDE : SN0;
+#elif FS_NCOR > 0
             FS_WSYNC();
             fs_cor_lags(C);
-#endif
 #endif
             FS_WSYNC();
         }
@@ -1152,7 +1268,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         if (mover) a.accepts[tid] = n_acc;
 #if FS_NOPS > 0
 #pragma unroll
-        for (int i = 0; i < (mover ? FS_NOPS : 0); i++) {
+        for (int i = 0; i < ((FS_PIPE ? grp == 1 : mover) ? FS_NOPS : 0); i++) {
             const size_t o = (size_t)tid * FS_NOPS + i;
 #if FS_ACCUM == 0
             ((FT *)a.op_means)[o] = FS_MUL(opr[i], (FT)FS_OPNORM);
@@ -1172,7 +1288,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         for (int c = 0; c < FS_NCOR; c++)
 #pragma unroll
             for (int j = 0; j < FS_LPT; j++) {
-                const int tau = lt + j * FS_CTPW;
+                const int tau = FS_LAG(j);
                 if (lagger && tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = cacc[c][j];
             }
 #endif

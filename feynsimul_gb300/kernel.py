@@ -19,7 +19,7 @@ from ._lib import FsConfig, FsInfo, check, lib, strings
 
 _ACCUM = {"fp32": _lib.ACCUM_REF_FP32, "fp64": _lib.ACCUM_FP64, "kahan": _lib.ACCUM_KAHAN,
           "study": _lib.ACCUM_STUDY}
-_COR_PARTIALS = {"fp32": _lib.FS_COR_PARTIALS_FP32, "float-float": _lib.FS_COR_PARTIALS_FLOAT_FLOAT}
+_PARTIALS = {"fp32": _lib.FS_PARTIALS_FP32, "exact": _lib.FS_PARTIALS_EXACT}
 
 
 def humanReadableSize(size):
@@ -69,7 +69,7 @@ class PIMCKernel:
         self._system = copy.copy(ka.system)
         self._compat = bool(getattr(ka, "compat", False))
         self._accumulation = getattr(ka, "accumulation", "fp64") or "fp64"
-        self._correlatorPartials = getattr(ka, "correlatorPartials", "fp32") or "fp32"
+        self._partials = getattr(ka, "partials", "fp32") or "fp32"
         self._fastMath = bool(getattr(ka, "fastMath", True))
         self._walkersPerBlock = int(getattr(ka, "walkersPerBlock", 0) or 0)
         self._seed = getattr(ka, "seed", None)
@@ -157,8 +157,8 @@ class PIMCKernel:
             raise NameError('metroStepsPerOperatorRun need to be set.')
         if self._accumulation not in _ACCUM:
             raise ValueError("accumulation must be one of " + ", ".join(_ACCUM))
-        if self._correlatorPartials not in _COR_PARTIALS:
-            raise ValueError("correlatorPartials must be one of " + ", ".join(_COR_PARTIALS))
+        if self._partials not in _PARTIALS:
+            raise ValueError("partials must be one of " + ", ".join(_PARTIALS))
 
         if self._enableParallelizePath:
             self._threadsPerWalker = self._N // (2 ** self._S)
@@ -193,7 +193,7 @@ class PIMCKernel:
         c.hist_bins = self._histBins
         c.compat = int(self._compat)
         c.accum = _ACCUM[self._accumulation]
-        c.cor_partials = _COR_PARTIALS[self._correlatorPartials]
+        c.partials = _PARTIALS[self._partials]
         c.fast_math = int(self._fastMath)
         c.walkers_per_block = self._walkersPerBlock
         c.min_blocks_per_sm = int(getattr(ka, "minBlocksPerSM", 0) or 0)

@@ -10,10 +10,12 @@ Keyword-only additions of this engine:
 * ``accumulation`` ("fp64"): operator / correlator running sums: "fp64", "fp32" (the
   reference's FP32 sums in its order), "kahan" (compensated FP32) or "study" (all three
   side by side, for the precision study).
-* ``correlatorPartials`` ("fp32"): how one measurement's correlator products of a lag are
-  summed before the FP64 add to the running sum ("fp64" and "kahan" accumulation of FP32
-  builds): "fp32" (four fused multiply-add chains, within gamma(N/4 + 2) * C(0) of the exact
-  sum) or "float-float" (the rounded products in float-float, about 48 bits).
+* ``partials`` ("fp32"): how one measurement's values are summed before their FP64 add to
+  the running sums (FP32 builds, "fp64" accumulation; the correlator also in "kahan"):
+  "fp32" (a thread's operator values over its slices in FP32, within gamma(2^S) of the
+  exact sum; a lag's products in four fused multiply-add chains, within
+  gamma(N/4 + 2) * C(0)) or "exact" (operator values added in FP64 one by one; the rounded
+  products in float-float, about 48 bits).  The "study" accumulation uses "exact".
 * ``fastMath`` (True): fast transcendental intrinsics, as the reference's
   ``-cl-fast-relaxed-math`` build; False gives IEEE functions and no FMA contraction.
 * ``histograms`` / ``histRange`` / ``histBins``: plugin expressions binned into one shared
@@ -66,7 +68,7 @@ class KernelArgs:
                  *,
                  compat=False,
                  accumulation="fp64",
-                 correlatorPartials="fp32",
+                 partials="fp32",
                  fastMath=True,
                  histograms=None,
                  histRange=None,
@@ -107,7 +109,7 @@ class KernelArgs:
         # additions
         self.compat = compat
         self.accumulation = accumulation
-        self.correlatorPartials = correlatorPartials
+        self.partials = partials
         self.fastMath = fastMath
         self.histograms = histograms
         self.histRange = histRange

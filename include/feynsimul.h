@@ -116,17 +116,19 @@ typedef struct fs_config {
     int32_t moves;
     double alpha;     /* single-node move width: node += alpha * (2u - 1) (kernel_args.py:124-126) */
     double ps_alpha;  /* path-shift width: offset = PSAlpha * (2u - 1) (kernel_args.py:128-131) */
-    /* new: how one measurement's correlator products of a lag are summed before the one
-     * FP64 add to the lag's running sum (FS_ACCUM_FP64 and FS_ACCUM_KAHAN in FP32 builds):
-     * FS_COR_PARTIALS_FP32 (0, default) = four FP32 fused multiply-add chains over the
-     * slices s mod 4, added pairwise; FS_COR_PARTIALS_FLOAT_FLOAT (1) = the rounded products
-     * summed in float-float (about 48 significant bits).  FS_ACCUM_STUDY always uses
-     * float-float for its FP64 column. */
-    int32_t cor_partials;
+    /* new: how one measurement's values are summed before their FP64 add to a running sum
+     * (FP32 builds; FS_ACCUM_FP64 for the operators, FS_ACCUM_FP64 and FS_ACCUM_KAHAN for
+     * the correlator).  FS_PARTIALS_FP32 (0, default): a thread's operator values of its
+     * slices summed in FP32 in slice order, then one FP64 add; a lag's products in four FP32
+     * fused multiply-add chains over the slices s mod 4, added pairwise, then one FP64 add.
+     * FS_PARTIALS_EXACT (1): every operator value added in FP64; the rounded products of a
+     * lag summed in float-float (about 48 significant bits).  FS_ACCUM_STUDY always uses
+     * the exact partials (its FP64 column is the study's reference). */
+    int32_t partials;
 } fs_config;
 
-#define FS_COR_PARTIALS_FP32 0
-#define FS_COR_PARTIALS_FLOAT_FLOAT 1
+#define FS_PARTIALS_FP32 0
+#define FS_PARTIALS_EXACT 1
 
 enum { FS_MOVE_BISECTION = 1, FS_MOVE_PATH_SHIFT = 2, FS_MOVE_SINGLE_NODE = 4 };
 
@@ -221,7 +223,7 @@ int fs_sync_timeout(fs_handle *h, double seconds);
  * double.  Correlator: [walkers][n_corr][N/2] running sums since creation / the last
  * fs_zero_accumulators, as double; FS_ACCUM_STUDY: [..][4] = plain FP32 sum, Kahan sum,
  * Kahan compensation, FP64 sum.  In FP32 builds every mode but FS_ACCUM_REF_FP32 sums one
- * measurement's products of a lag in FP32 (fs_config.cor_partials) before adding them to
+ * measurement's products of a lag in FP32 (fs_config.partials) before adding them to
  * the lag's FP64 running sum.  Bins: [res^DOF] counts.  Histogram: [hist_bins] counts. */
 int fs_get_operators(fs_handle *h, double *out, size_t n);
 int fs_get_correlator(fs_handle *h, double *out, size_t n);

@@ -56,7 +56,7 @@ def _compile(cfg, pot, uc="", ops=(), cors=(), hists=()):
     dict(enable_parallelize_path=0, walkers_per_group=1),
     dict(enable_double=1, accum=3),
     dict(n_slices=2048, bisection_level=2, n_walkers=4),   # 512 threads per walker
-    dict(cor_partials=1),                                   # float-float correlator partials
+    dict(partials=1),                                       # exact partials
     dict(accum=2, enable_parallelize_path=0, walkers_per_group=1),  # FMA partials, one lag loop
     dict(n_slices=2, bisection_level=1),                    # N not a multiple of 4
 ])

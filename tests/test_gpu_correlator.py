@@ -21,7 +21,7 @@ from gpu_util import engine, require_gpu
 pytestmark = pytest.mark.gpu
 
 
-def _kernel(partials, parallel, N, S, W=256, wpb=0):
+def _kernel(partials, parallel, N, S, W=256, wpb=0, fast=True):
     kernel, kernel_args = engine()
     sysm = types.SimpleNamespace(DOF=1, potential="0.5 * x1 * x1", userCode="")
     ka = kernel_args.KernelArgs(
@@ -29,21 +29,22 @@ def _kernel(partials, parallel, N, S, W=256, wpb=0):
         enableBisection=True, enablePathShift=False, enableSingleNodeMove=False, enableBins=False,
         nbrOfWalkersPerWorkGroup=1, enableParallelizePath=parallel, enableGlobalPath=False,
         enableGlobalOldPath=False, operators=("x1 * x1",), correlators=("x1", "x1 * x1 - 0.5"),
-        operatorRuns=6, metroStepsPerOperatorRun=2, correlatorPartials=partials, walkersPerBlock=wpb,
-        seed=11)
+        operatorRuns=6, metroStepsPerOperatorRun=2, partials=partials, walkersPerBlock=wpb,
+        fastMath=fast, seed=11)
     return kernel.PIMCKernel(ka)
 
 
-@pytest.mark.parametrize("parallel,N,S", [
-    (True, 128, 3),    # 16 segment threads + 48 helper threads, one lag each
-    (True, 64, 2),     # 16 segment threads + 16 helpers, one lag each
-    (True, 256, 2),    # 64 segment threads, two lags each, no helpers
-    (False, 64, 2),    # one thread per walker: all 32 lags in one loop, sums in device memory
-], ids=["helpers4", "helpers2", "two_lags", "walker_mode"])
-def test_fp32_partials_within_bound_of_float_float(parallel, N, S):
+@pytest.mark.parametrize("parallel,N,S,wpb", [
+    (True, 128, 3, 0),   # 16 segment threads + 32 pipelined helpers, a lane pair per 4 lags
+    (True, 64, 2, 0),    # 16 segment threads + 16 pipelined helpers, a lane pair per 4 lags
+    (True, 128, 3, 1),   # movers in half warps: 16 + 48 helpers after the moves, one lag each
+    (True, 256, 2, 0),   # 64 segment threads, two lags each, no helpers
+    (False, 64, 2, 0),   # one thread per walker: all 32 lags in one loop, sums in device memory
+], ids=["pipelined", "pipelined_n64", "helpers", "two_lags", "walker_mode"])
+def test_fp32_partials_within_bound_of_float_float(parallel, N, S, wpb):
     require_gpu()
     W = 256
-    kf, kx = _kernel("fp32", parallel, N, S, W), _kernel("float-float", parallel, N, S, W)
+    kf, kx = _kernel("fp32", parallel, N, S, W, wpb), _kernel("exact", parallel, N, S, W, wpb)
     p0 = (np.random.RandomState(5).randn(W, N) * 0.7).astype(np.float32)
     for k in (kf, kx):
         k.setPaths(p0)
@@ -65,17 +66,23 @@ def test_fp32_partials_within_bound_of_float_float(parallel, N, S):
     kx.close()
 
 
-@pytest.mark.parametrize("partials", ["fp32", "float-float"])
-def test_pipelined_helpers_bit_identical(partials):
+def test_pipelined_helpers_bit_identical():
     """The launch shapes of one HO run (N = 128, S = 3: 16 segment threads per walker):
-    2 walkers per CTA pipeline 64 helper threads per walker one measurement behind the
-    movers; 1 walker per CTA leaves the movers in half warps, so every thread of 4 groups
-    sums lags after the moves.  Each lag is summed by one thread in the same order either
-    way, so paths, operators, accepts and correlator sums are bit-identical."""
+    2 walkers per CTA pipeline 32 helper threads per walker (a pair of lanes per 4 lags; the
+    operators and correlator values on a path snapshot) one measurement behind the movers;
+    1 walker per CTA
+    leaves the movers in half warps, so every thread of 4 groups sums one lag after the
+    moves, and the movers evaluate the operators.  Each sum is formed by one thread in the
+    same order either way, so paths, operators, accepts and correlator sums are
+    bit-identical.  IEEE builds:
+    with contraction allowed, the compiler may fuse x1 * x1 - 0.5 into one FMA at one call
+    site and not at another, and the two shapes evaluate it at different call sites."""
     require_gpu()
     W, N = 256, 128
-    kp, kh = _kernel(partials, True, N, 3, W, wpb=2), _kernel(partials, True, N, 3, W, wpb=1)
-    assert kp._info.block_threads == 2 * 16 * 5 and kh._info.block_threads == 16 * 4
+    kp = _kernel("fp32", True, N, 3, W, wpb=2, fast=False)
+    kh = _kernel("fp32", True, N, 3, W, wpb=1, fast=False)
+    assert (kp._info.walkers_per_block, kp._info.block_threads) == (2, 2 * 16 * 3)
+    assert (kh._info.walkers_per_block, kh._info.block_threads) == (1, 16 * 4)
     p0 = (np.random.RandomState(6).randn(W, N) * 0.7).astype(np.float32)
     for k in (kp, kh):
         k.setPaths(p0)

@@ -41,7 +41,7 @@ def _kernel(sysm, walkers, N, S, global_path, double=False, accumulation="fp64",
         enableRanlux=ranlux, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
         operators=(sysm.energyOp,), correlators=(hyperradius2(sysm.DOF),), operatorRuns=op_runs,
         metroStepsPerOperatorRun=msteps, accumulation=accumulation, fastMath=fast, seed=seed,
-        correlatorPartials=partials)
+        partials=partials)
     k = kernel.PIMCKernel(ka)
     if ranlux:
         k.initRanlux()
@@ -107,7 +107,7 @@ def test_study_columns_and_device_moments():
     # round the operator expression differently
     ks = _kernel(sysm, W, N, S, True, accumulation="study", fast=False)
     # the study's FP64 column sums each measurement in float-float
-    kd = _kernel(sysm, W, N, S, True, accumulation="fp64", fast=False, partials="float-float")
+    kd = _kernel(sysm, W, N, S, True, accumulation="fp64", fast=False, partials="exact")
     p0 = sysm.initial_paths(W, N, np.random.RandomState(4)).astype(np.float32)
     for k in (ks, kd):
         k.setPaths(p0)
