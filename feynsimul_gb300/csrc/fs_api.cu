@@ -644,8 +644,8 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
         // Where the movers of a CTA fill whole warps (walker count and walkers per CTA
         // multiples of 32 / threads per walker) the helpers are pipelined (FS_PIPE): the
         // movers copy their slices to a double-buffered path snapshot, and the helpers alone
-        // evaluate the operators and correlator values on it and sum the lags, one
-        // measurement behind the moves.
+        // evaluate the correlator values on it and sum the lags, one measurement behind the
+        // moves.
         // The pipelined helpers give each pair of threads 4 consecutive lags (N/4 lag threads
         // per walker, in pairs of one walker: an even number of segment threads) and sum
         // FP32 partials over the doubled slice values.

@@ -28,14 +28,13 @@
 // moves and the per-slice measurement; every group sums correlator lags, so a walker's N/2
 // lags spread over FS_TPW x FS_MX threads instead of its FS_TPW segment threads.  Each lag is
 // still summed by one thread in slice order, so the sums are the same bit for bit.
-// FS_PIPE (the host sets it where the movers fill whole warps): the movers measure by
-// copying their slices into a double-buffered path snapshot (FS_SNSTRIDE words each, the
-// padded slice layout); the helper groups evaluate the operators (group 1, for the segment
-// of the same index, in the mover's order) and the correlator values on the snapshot and
-// sum the lags, for measurement m while the movers sweep towards measurement m + 1.  One CTA
-// barrier per measurement hands a snapshot over; the movers sync among themselves on named
-// barrier 1 and the helpers on named barrier 2.  Every sum is formed by one thread in the
-// same order as without the pipeline, so the results are the same bit for bit.
+// FS_PIPE (the host sets it where the movers fill whole warps): the movers measure the
+// operators and copy their slices into a double-buffered path snapshot (FS_SNSTRIDE words
+// each, the padded slice layout); the helper groups evaluate the correlator values on the
+// snapshot and sum the lags, for measurement m while the movers sweep towards measurement
+// m + 1.  One CTA barrier per measurement hands a snapshot over; the movers sync among
+// themselves on named barrier 1 and the helpers on named barrier 2.  Every sum is formed in
+// the same order as without the pipeline, so the results are the same bit for bit.
 #ifndef FS_MX
 #define FS_MX 1
 #endif
@@ -1073,7 +1072,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #pragma unroll
                     for (int j = 0; j < 4; j++) pa[j][0] = pa[j][1] = 0.0f;
                     float2 w0 = wv2[0];
-#pragma unroll 4
+#pragma unroll 32
                     for (int q = 0; q < FS_N / 4; q++) {
                         const float2 a2 = cv2[2 * q + h];
                         const float2 w1 = wv2[2 * q + 1], w2 = wv2[2 * q + 2];
@@ -1114,13 +1113,6 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             for (int run = 0; run < FS_OPRUNS; run++) {
                 __syncthreads();
                 const FT *Q = SN0 + (run & 1) * FS_SNSTRIDE;
-#if FS_NOPS > 0
-                if (grp == 1) {
-#pragma unroll 1
-                    for (int s = t * FS_SEG; s < (t + 1) * FS_SEG; s++) fs_op_add(Q, s);
-                    fs_op_flush();
-                }
-#endif
 #pragma unroll 1
                 for (int s = lt; s < FS_N; s += FS_CTPW) fs_cor_put(Q, s);
                 asm volatile("bar.sync 2, %0;" ::"n"(FS_BLOCK - FS_MBLOCK) : "memory");
@@ -1211,16 +1203,14 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #endif
 #pragma unroll 1
             for (int s = s_lo; s < (mover ? s_hi : s_lo); s++) {
-#if FS_PIPE
-#pragma unroll
-                for (int d = 0; d < FS_DOF; d++) FS_AT(SN, d, s) = FS_AT(P, d, s);
-#else
 #if FS_NOPS > 0
                 fs_op_add(P, s);
 #endif
-#if FS_NCOR > 0
+#if FS_PIPE
+#pragma unroll
+                for (int d = 0; d < FS_DOF; d++) FS_AT(SN, d, s) = FS_AT(P, d, s);
+#elif FS_NCOR > 0
                 fs_cor_put(P, s);
-#endif
 #endif
 #if FS_BINS
                 {
@@ -1250,7 +1240,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                 }
 #endif
             }
-#if FS_NOPS > 0 && !FS_PIPE
+#if FS_NOPS > 0
             if (mover) fs_op_flush();
 #endif
 #if FS_PIPE
@@ -1268,7 +1258,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         if (mover) a.accepts[tid] = n_acc;
 #if FS_NOPS > 0
 #pragma unroll
-        for (int i = 0; i < ((FS_PIPE ? grp == 1 : mover) ? FS_NOPS : 0); i++) {
+        for (int i = 0; i < (mover ? FS_NOPS : 0); i++) {
             const size_t o = (size_t)tid * FS_NOPS + i;
 #if FS_ACCUM == 0
             ((FT *)a.op_means)[o] = FS_MUL(opr[i], (FT)FS_OPNORM);

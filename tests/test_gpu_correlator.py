@@ -68,13 +68,11 @@ def test_fp32_partials_within_bound_of_float_float(parallel, N, S, wpb):
 
 def test_pipelined_helpers_bit_identical():
     """The launch shapes of one HO run (N = 128, S = 3: 16 segment threads per walker):
-    2 walkers per CTA pipeline 32 helper threads per walker (a pair of lanes per 4 lags; the
-    operators and correlator values on a path snapshot) one measurement behind the movers;
-    1 walker per CTA
-    leaves the movers in half warps, so every thread of 4 groups sums one lag after the
-    moves, and the movers evaluate the operators.  Each sum is formed by one thread in the
-    same order either way, so paths, operators, accepts and correlator sums are
-    bit-identical.  IEEE builds:
+    2 walkers per CTA pipeline 32 helper threads per walker (a pair of lanes per 4 lags, the
+    correlator values from a path snapshot) one measurement behind the movers; 1 walker per
+    CTA leaves the movers in half warps, so every thread of 4 groups sums one lag after the
+    moves.  Each sum is formed in the same order either way, so paths, operators, accepts
+    and correlator sums are bit-identical.  IEEE builds:
     with contraction allowed, the compiler may fuse x1 * x1 - 0.5 into one FMA at one call
     site and not at another, and the two shapes evaluate it at different call sites."""
     require_gpu()
