@@ -745,6 +745,7 @@ def main():
     ap.add_argument("--no-ess", action="store_true", help="skip the energy ESS/s measurement")
     ap.add_argument("--ess-launches", type=int, default=200, help="measurements per walker of the ESS loop")
     ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch sub-record of the default run")
+    ap.add_argument("--no-ho", action="store_true", help="skip the harmonic-oscillator sub-record of the default run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -812,6 +813,18 @@ def main():
             result["ragged_batch"] = {k: br[k] for k in ("metric", "value", "unit", "ms_per_step", "steps",
                                                          "roofline", "clocks", "config", "gpu_launches",
                                                          "cpu_baseline") if k in br}
+        if args.config == "he3" and not args.no_ho and world == 1:
+            # config 1 (1D HO, correlator every sweep) as a sub-record, same timing rules
+            hargs = argparse.Namespace(**vars(args))
+            hargs.config, hargs.no_ess = "ho", True
+            hargs.walkers = hargs.op_runs = hargs.msteps = hargs.S = hargs.wpb = 0
+            hargs.minb = -1
+            hr, hctx = run_gb300(hargs, 0, 1)
+            hrec = {k: hr[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "config", "launch",
+                                       "e2e", "roofline", "clocks", "gpu_launches", "acceptance_rate")}
+            if not args.no_cpu_baseline:
+                hrec["cpu_baseline"] = oracle_cpu_rate(*hctx[:3], seconds=min(args.cpu_seconds, 4.0))
+            result["harmonic_oscillator"] = hrec
         print(json.dumps(_json_safe(result)))
     if world > 1:
         import torch.distributed as dist
