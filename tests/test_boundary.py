@@ -57,6 +57,7 @@ def _compile(cfg, pot, uc="", ops=(), cors=(), hists=()):
     dict(enable_double=1, accum=3),
     dict(n_slices=2048, bisection_level=2, n_walkers=4),   # 512 threads per walker
     dict(partials=1),                                       # exact partials
+    dict(accum=2),                                          # Kahan operators, pipelined lags
     dict(accum=2, enable_parallelize_path=0, walkers_per_group=1),  # FMA partials, one lag loop
     dict(n_slices=2, bisection_level=1),                    # N not a multiple of 4
 ])
@@ -65,6 +66,14 @@ def test_nvrtc_compiles_for_sm103a(kw):
                        ("1.0 * x1 * x1", "native_exp(-sqr(x1))"), ("x1",))
     assert rc == 0, log
     assert "fs_metropolis" in log
+
+
+def test_nvrtc_compiles_five_correlators():
+    # the pipelined lag sums of more correlators than fit in registers (running sums in
+    # device memory)
+    rc, log = _compile(_cfg(), "0.5 * 1.0 * x1 * x1", "", ("1.0 * x1 * x1",),
+                       ("x1", "x1 * x1", "x1 * x1 * x1", "0.5 * x1", "x1 - 1.0"))
+    assert rc == 0, log
 
 
 def test_lm2m2_plugin_compiles():

@@ -21,16 +21,21 @@ from gpu_util import engine, require_gpu
 pytestmark = pytest.mark.gpu
 
 
-def _kernel(partials, parallel, N, S, W=256, wpb=0, fast=True):
+COR2 = ("x1", "x1 * x1 - 0.5")
+# five correlators: more than the lag sums keep in registers (4 lags x 4 correlators)
+COR5 = ("x1", "x1 * x1 - 0.5", "x1 * x1 * x1", "0.5 * x1 + 0.25", "x1 * x1 * x1 * x1 - 0.75")
+
+
+def _kernel(partials, parallel, N, S, W=256, wpb=0, fast=True, cors=COR2, accumulation="fp64"):
     kernel, kernel_args = engine()
     sysm = types.SimpleNamespace(DOF=1, potential="0.5 * x1 * x1", userCode="")
     ka = kernel_args.KernelArgs(
         system=sysm, nbrOfWalkers=W, N=N, beta=10.0, S=S, enableOperator=True, enableCorrelator=True,
         enableBisection=True, enablePathShift=False, enableSingleNodeMove=False, enableBins=False,
         nbrOfWalkersPerWorkGroup=1, enableParallelizePath=parallel, enableGlobalPath=False,
-        enableGlobalOldPath=False, operators=("x1 * x1",), correlators=("x1", "x1 * x1 - 0.5"),
+        enableGlobalOldPath=False, operators=("x1 * x1",), correlators=cors,
         operatorRuns=6, metroStepsPerOperatorRun=2, partials=partials, walkersPerBlock=wpb,
-        fastMath=fast, seed=11)
+        fastMath=fast, accumulation=accumulation, seed=11)
     return kernel.PIMCKernel(ka)
 
 
@@ -66,7 +71,9 @@ def test_fp32_partials_within_bound_of_float_float(parallel, N, S, wpb):
     kx.close()
 
 
-def test_pipelined_helpers_bit_identical():
+@pytest.mark.parametrize("cors,accumulation", [(COR2, "fp64"), (COR5, "fp64"), (COR2, "kahan")],
+                         ids=["two_correlators", "five_correlators", "kahan"])
+def test_pipelined_helpers_bit_identical(cors, accumulation):
     """The launch shapes of one HO run (N = 128, S = 3: 16 segment threads per walker):
     2 walkers per CTA pipeline 32 helper threads per walker (a pair of lanes per 4 lags, the
     correlator values from a path snapshot) one measurement behind the movers; 1 walker per
@@ -77,8 +84,8 @@ def test_pipelined_helpers_bit_identical():
     site and not at another, and the two shapes evaluate it at different call sites."""
     require_gpu()
     W, N = 256, 128
-    kp = _kernel("fp32", True, N, 3, W, wpb=2, fast=False)
-    kh = _kernel("fp32", True, N, 3, W, wpb=1, fast=False)
+    kp = _kernel("fp32", True, N, 3, W, wpb=2, fast=False, cors=cors, accumulation=accumulation)
+    kh = _kernel("fp32", True, N, 3, W, wpb=1, fast=False, cors=cors, accumulation=accumulation)
     assert (kp._info.walkers_per_block, kp._info.block_threads) == (2, 2 * 16 * 3)
     assert (kh._info.walkers_per_block, kh._info.block_threads) == (1, 16 * 4)
     p0 = (np.random.RandomState(6).randn(W, N) * 0.7).astype(np.float32)
