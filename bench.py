@@ -817,6 +817,9 @@ def main():
             # config 1 (1D HO, correlator every sweep) as a sub-record, same timing rules
             hargs = argparse.Namespace(**vars(args))
             hargs.config, hargs.no_ess = "ho", True
+            # a launch is ~0.14 ms: 3000 of them give the clock sampler (200 ms period) a
+            # timed region to sample
+            hargs.steps = max(args.steps, 3000)
             hargs.walkers = hargs.op_runs = hargs.msteps = hargs.S = hargs.wpb = 0
             hargs.minb = -1
             hr, hctx = run_gb300(hargs, 0, 1)
