@@ -159,8 +159,13 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
                 }
                 fs_walker_sync(tpw, wl);
             }
-            // ---- measurement: the thread's slices (kernel.c:734-745) ----
+            // ---- measurement: the thread's slices (kernel.c:734-745), summed in FP32 in
+            // slice order and then added once to the FP64 sums (a chain of FP64 adds per
+            // slice is slow on GB300's narrow FP64 pipe) ----
             if (Sys::NOPS > 0) {
+                float opp[Sys::NOPS > 0 ? Sys::NOPS : 1];
+#pragma unroll
+                for (int k = 0; k < Sys::NOPS; k++) opp[k] = 0.0f;
 #pragma unroll 1
                 for (int s = t * seg; s < (t + 1) * seg; s++) {
                     float x[DOF], ov[Sys::NOPS > 0 ? Sys::NOPS : 1];
@@ -168,8 +173,10 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
                     for (int d = 0; d < DOF; d++) x[d] = FSB_AT(P, d, s);
                     Sys::ops(x, ov);
 #pragma unroll
-                    for (int k = 0; k < Sys::NOPS; k++) opd[k] += (double)ov[k];
+                    for (int k = 0; k < Sys::NOPS; k++) opp[k] = __fadd_rn(opp[k], ov[k]);
                 }
+#pragma unroll
+                for (int k = 0; k < Sys::NOPS; k++) opd[k] += (double)opp[k];
             }
             fs_walker_sync(tpw, wl);
         }
