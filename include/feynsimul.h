@@ -83,7 +83,9 @@ typedef struct fs_config {
     /* new: histogram of plugin expressions (e.g. pair distances), shared bins */
     double hist_lo, hist_hi;
     int32_t hist_bins;
-    /* new: 1 = reference-compatible RNG use (see DESIGN), 0 = fixed */
+    /* new: 1 = reference-compatible random-number use (per-thread xorshift rows whose walker
+     * stream is never written back, kernel.c:568-572; RANLUX tables all seeded from seeds[0],
+     * kernel.c:155; RANLUX integers with zero low bits, kernel.c:206), 0 = fixed */
     int32_t compat;
     /* new: FS_ACCUM_* */
     int32_t accum;
