@@ -1,6 +1,7 @@
-// fs_mlp.cuh -- the learned bisection proposal's network on the tensor cores (BF16 inputs,
-// FP32 accumulation, mma.sync.m16n8k16).  Shared by the sampler (pasted into the NVRTC
-// module when the learned proposal is on) and by the training kernels (fs_mlp_train.cu).
+// fs_mlp.cuh -- the learned bisection proposal's network evaluated per warp on the tensor
+// cores (BF16 inputs, FP32 accumulation, mma.sync.m16n8k16) inside the sweep, pasted into
+// the NVRTC module when the learned proposal is on; its sizes and BF16 packing are shared
+// with the tcgen05 training and batched-inference kernels (fs_mlp_train.cu, fs_mlp_tc.cu).
 // No counterpart in the reference.
 //
 // Network: 4 linear layers 16 -> 128 -> 128 -> 128 -> 16 with ReLU between them.

@@ -20,13 +20,11 @@
 
 #include "../../include/feynsimul.h"
 #include "fs_mlp.cuh"
-
-typedef unsigned short fs_bf16;
+#include "fs_tc.cuh"
 
 #define TC_M 128                  // rows per tile (the MMA's M)
 #define TC_THREADS 128            // 4 warps
 #define TC_TMEM_COLS 128          // FP32 accumulator columns (N <= 128)
-#define TC_SPIN_LIMIT (1u << 20)  // try_wait polls before a CTA gives up
 
 extern int fsi_thread_error(int code, const char *msg);
 
@@ -41,89 +39,6 @@ struct TcSmem {
     unsigned tmem_base;
     int give_up;
 };
-
-// element offset of (row r, column k) in a K-major canonical tile with K columns
-__device__ __forceinline__ int tc_off(int r, int k, int K)
-{
-    return (r >> 3) * (K * 8) + (k >> 3) * 64 + (r & 7) * 8 + (k & 7);
-}
-
-__device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// shared-memory matrix descriptor: start address, leading byte offset 128 (next core matrix
-// along K), stride byte offset K * 16 (next 8-row group), descriptor version 1, no swizzle
-__device__ __forceinline__ uint64_t tc_desc(const fs_bf16 *start, int K)
-{
-    const uint64_t a = (tc_smem(start) >> 4) & 0x3FFFu;
-    const uint64_t lbo = 128u >> 4, sbo = ((uint64_t)K * 16u) >> 4;
-    return a | (lbo << 16) | (sbo << 32) | (1ull << 46);
-}
-
-// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major
-__device__ __forceinline__ uint32_t tc_idesc(int M, int N)
-{
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate)
-{
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                 ::"r"(d), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
-                 : "memory");
-}
-
-__device__ __forceinline__ void tc_commit(uint32_t mbar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
-                 : "memory");
-}
-
-// bounded wait for the barrier phase with this parity; false when the limit is reached
-__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity)
-{
-    for (uint32_t i = 0; i < TC_SPIN_LIMIT; i++) {
-        uint32_t done;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(done)
-                     : "r"(mbar), "r"(parity)
-                     : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-// generic-proxy shared-memory writes made visible to the tensor cores' reads
-__device__ __forceinline__ void tc_fence_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-// 16 FP32 accumulator columns of this thread's TMEM lane, the load completed before return
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
-{
-    uint32_t r[16];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                 "[%16];\n\ttcgen05.wait::ld.sync.aligned;"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                   "=r"(r[15])
-                 : "r"(taddr)
-                 : "memory");
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-
-// eight BF16 values (k .. k+7 of one row) as one 16-byte shared store
-__device__ __forceinline__ void tc_st8(fs_bf16 *dst, const float *h)
-{
-    uint4 u;
-    u.x = fs_pack_bf16(h[0], h[1]);
-    u.y = fs_pack_bf16(h[2], h[3]);
-    u.z = fs_pack_bf16(h[4], h[5]);
-    u.w = fs_pack_bf16(h[6], h[7]);
-    *(uint4 *)dst = u;
-}
 
 // one layer's weights, fragment order -> canonical K-major layout [N][K]
 __device__ __forceinline__ void tc_unpack(fs_bf16 *w, const uint2 *__restrict__ frag, int K, int N)

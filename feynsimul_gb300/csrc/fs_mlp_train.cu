@@ -1,20 +1,25 @@
-// fs_mlp_train.cu -- training and inference kernels of the learned bisection proposal
-// (BF16 tensor-core mma.sync, FP32 accumulation).  No counterpart in the reference.
+// fs_mlp_train.cu -- training of the learned bisection proposal's network on the tcgen05
+// tensor cores (BF16 operands, FP32 accumulation in tensor memory), its Adam step and weight
+// packing, and the C ABI of training and batched inference.  No counterpart in the
+// reference.
 //
 // Parameters (FP32 master copy, one flat array, FS_MLP_NPARAM floats):
 //   W1[128][16] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] W4[16][128] b4[16]
-// Training tile: 64 rows per CTA, 8 warps.  Forward keeps the BF16 activations in shared
-// memory; the loss gradient is formed per row; backward runs dW = dZ^T A and dA = dZ W with
-// transposed ldmatrix loads and adds the CTA's weight / bias gradients to an FP32 gradient
-// array with atomics (the Adam kernel divides nothing: the loss is already a batch mean).
+// The forward pass keeps the BF16 activations in shared memory; the loss gradient is formed
+// per row; the backward pass runs dA = dZ W and dW = dZ^T A and adds the weight / bias
+// gradients to an FP32 gradient array with atomics (the Adam kernel divides nothing: the
+// loss is already a batch mean).
 //
 // Loss (per row, D degrees of freedom, z the midpoint's displacement from the endpoints'
 // mean in units of sigma_1): sum_d 0.5 (z_d - o_d)^2 exp(-s_d) + 0.5 s_d with
 // s_d = 4 tanh(o_{D+d} / 4): the Gaussian negative log-likelihood of z under N(o, exp(s)).
 #include <cuda_runtime.h>
 
+#include <stddef.h>
+
 #include "../../include/feynsimul.h"
 #include "fs_mlp.cuh"
+#include "fs_tc.cuh"
 
 #define FS_MLP_NPARAM (128 * 16 + 128 + 128 * 128 + 128 + 128 * 128 + 128 + 16 * 128 + 16)
 #define P_W1 0
@@ -33,32 +38,7 @@
 #define Q_W4 (Q_W3 + 128 * 128)
 #define Q_N (Q_W4 + 16 * 128)
 
-typedef unsigned short fs_bf16;  // raw BF16 bits
-
-#define ROWS 64
-#define LDH 136  // padded row stride (elements) of 128-wide tiles
-#define LDS 24   // padded row stride of 16-wide tiles
-
 extern int fsi_thread_error(int code, const char *msg);
-
-__device__ __forceinline__ unsigned smem_addr(const void *p)
-{
-    return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const fs_bf16 *p)
-{
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_addr(p)));
-}
-
-__device__ __forceinline__ void ldsm_x4_t(unsigned (&r)[4], const fs_bf16 *p)
-{
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_addr(p)));
-}
 
 __device__ __forceinline__ fs_bf16 f2bf(float x)
 {
@@ -66,282 +46,317 @@ __device__ __forceinline__ fs_bf16 f2bf(float x)
     return (fs_bf16)(r & 0xFFFFu);
 }
 
-__device__ __forceinline__ float bf2f(fs_bf16 x) { return __uint_as_float(((unsigned)x) << 16); }
+// ---------------------------------------------------------------- tcgen05 training
+// The same forward pass, loss and backward pass on the fifth-generation tensor cores, with
+// the same BF16 rounding points.  One CTA = 4 warps, persistent over 128-row tiles; thread t
+// owns row t of a tile (tensor-memory lane t) in every epilogue.  Tensor memory (512 FP32
+// columns): the layer accumulator F (a forward layer's output or a hidden gradient dA), and
+// the weight gradients summed over the CTA's tiles: dW2 and dW3 (128 columns each), dW1 (16)
+// and dW4 transposed (16; its M is the 128 inputs).  Shared memory holds BF16 tiles in the
+// canonical layout of fs_tc.cuh: the activations a1..a3 and the hidden gradient g (128 x
+// 128, rows = the tile's rows), the input x and the output gradient dz4 (128 x 16), and the
+// weights W1..W4 ([out][in]).  The forward GEMMs read them K-major; dA = dZ W reads W
+// MN-major, and dW = dZ^T A reads dZ and A MN-major (K = the tile's rows), so no tile is
+// transposed.  The six 128-wide tiles come first and the allocation is padded, so every
+// byte a descriptor can reach lies inside it under either reading of its byte offsets.
+// Bias gradients are FP32 column sums of the unrounded gradients (warp butterflies, then
+// shared-memory atomics).
+#define TT_THREADS 128
+#define TT_TMEM_COLS 512
+#define TT_F 0u
+#define TT_DW2 128u
+#define TT_DW3 256u
+#define TT_DW1 384u
+#define TT_DW4 400u
 
-// acc[MT][NT] += A * B over K for one warp.
-//   TA = false: A stored A[m][k] (k contiguous);  TA = true: stored At[k][m].
-//   TB = false: B stored Bt[n][k] (k contiguous); TB = true: stored B[k][n].
-// NT must be even (two n-tiles per ldmatrix.x4).
-template <int MT, int NT, bool TA, bool TB>
-__device__ __forceinline__ void warp_gemm(float (&acc)[MT][NT][4], const fs_bf16 *A, int lda, int m0,
-                                          const fs_bf16 *B, int ldb, int n0, int K, int lane)
-{
-    const int j = lane >> 3, r8 = lane & 7;
-    for (int k0 = 0; k0 < K; k0 += 16) {
-        unsigned a[MT][4];
-#pragma unroll
-        for (int mt = 0; mt < MT; mt++) {
-            if (!TA)
-                ldsm_x4(a[mt], A + (m0 + mt * 16 + r8 + (j & 1) * 8) * lda + k0 + (j >> 1) * 8);
-            else
-                ldsm_x4_t(a[mt], A + (k0 + (j >> 1) * 8 + r8) * lda + m0 + mt * 16 + (j & 1) * 8);
-        }
-#pragma unroll
-        for (int nt = 0; nt < NT; nt += 2) {
-            unsigned b[4];
-            if (!TB)
-                ldsm_x4(b, B + (n0 + nt * 8 + (j >> 1) * 8 + r8) * ldb + k0 + (j & 1) * 8);
-            else
-                ldsm_x4_t(b, B + (k0 + (j & 1) * 8 + r8) * ldb + n0 + nt * 8 + (j >> 1) * 8);
-#pragma unroll
-            for (int mt = 0; mt < MT; mt++) {
-                fs_mma_bf16(acc[mt][nt], a[mt][0], a[mt][1], a[mt][2], a[mt][3], b[0], b[1]);
-                fs_mma_bf16(acc[mt][nt + 1], a[mt][0], a[mt][1], a[mt][2], a[mt][3], b[2], b[3]);
-            }
-        }
-    }
-}
-
-template <int MT, int NT>
-__device__ __forceinline__ void zero_acc(float (&acc)[MT][NT][4])
-{
-#pragma unroll
-    for (int i = 0; i < MT; i++)
-#pragma unroll
-        for (int j = 0; j < NT; j++) acc[i][j][0] = acc[i][j][1] = acc[i][j][2] = acc[i][j][3] = 0.f;
-}
-
-// forward epilogue: out = relu(acc + bias) as BF16 into a [ROWS][LDH] tile
-template <int NT>
-__device__ __forceinline__ void store_relu(const float (&acc)[1][NT][4], const float *bias, fs_bf16 *out, int m0,
-                                           int n0, int lane)
-{
-    const int r = m0 + (lane >> 2), c = (lane & 3) * 2;
-#pragma unroll
-    for (int nt = 0; nt < NT; nt++) {
-        const int col = n0 + nt * 8 + c;
-        const float b0 = bias[col], b1 = bias[col + 1];
-        out[r * LDH + col] = f2bf(fmaxf(acc[0][nt][0] + b0, 0.f));
-        out[r * LDH + col + 1] = f2bf(fmaxf(acc[0][nt][1] + b1, 0.f));
-        out[(r + 8) * LDH + col] = f2bf(fmaxf(acc[0][nt][2] + b0, 0.f));
-        out[(r + 8) * LDH + col + 1] = f2bf(fmaxf(acc[0][nt][3] + b1, 0.f));
-    }
-}
-
-// backward epilogue: dZ = acc * (A > 0) as BF16, column sums of dZ into the bias gradient
-template <int NT>
-__device__ __forceinline__ void store_dz(const float (&acc)[1][NT][4], const fs_bf16 *act, fs_bf16 *out,
-                                         float *s_db, int m0, int n0, int lane)
-{
-    const int r = m0 + (lane >> 2), c = (lane & 3) * 2;
-#pragma unroll
-    for (int nt = 0; nt < NT; nt++) {
-        const int col = n0 + nt * 8 + c;
-        float v[4];
-        v[0] = bf2f(act[r * LDH + col]) > 0.f ? acc[0][nt][0] : 0.f;
-        v[1] = bf2f(act[r * LDH + col + 1]) > 0.f ? acc[0][nt][1] : 0.f;
-        v[2] = bf2f(act[(r + 8) * LDH + col]) > 0.f ? acc[0][nt][2] : 0.f;
-        v[3] = bf2f(act[(r + 8) * LDH + col + 1]) > 0.f ? acc[0][nt][3] : 0.f;
-        out[r * LDH + col] = f2bf(v[0]);
-        out[r * LDH + col + 1] = f2bf(v[1]);
-        out[(r + 8) * LDH + col] = f2bf(v[2]);
-        out[(r + 8) * LDH + col + 1] = f2bf(v[3]);
-        // sum the 16 rows of this fragment column: lanes with equal (lane & 3)
-        float s0 = v[0] + v[2], s1 = v[1] + v[3];
-#pragma unroll
-        for (int off = 4; off < 32; off <<= 1) {
-            s0 += __shfl_xor_sync(0xFFFFFFFFu, s0, off);
-            s1 += __shfl_xor_sync(0xFFFFFFFFu, s1, off);
-        }
-        if (lane < 4) {
-            atomicAdd(s_db + col, s0);
-            atomicAdd(s_db + col + 1, s1);
-        }
-    }
-}
-
-// weight-gradient epilogue: atomically add a warp tile of dW[o][i] (row stride ld)
-template <int MT, int NT>
-__device__ __forceinline__ void add_dw(const float (&acc)[MT][NT][4], float *g, int ld, int m0, int n0, int lane)
-{
-    const int r = lane >> 2, c = (lane & 3) * 2;
-#pragma unroll
-    for (int mt = 0; mt < MT; mt++)
-#pragma unroll
-        for (int nt = 0; nt < NT; nt++) {
-            const int row = m0 + mt * 16 + r, col = n0 + nt * 8 + c;
-            atomicAdd(g + row * ld + col, acc[mt][nt][0]);
-            atomicAdd(g + row * ld + col + 1, acc[mt][nt][1]);
-            atomicAdd(g + (row + 8) * ld + col, acc[mt][nt][2]);
-            atomicAdd(g + (row + 8) * ld + col + 1, acc[mt][nt][3]);
-        }
-}
-
-struct __align__(16) MlpSmem {
-    fs_bf16 w1[128 * LDS];
-    fs_bf16 w2[128 * LDH];
-    fs_bf16 w3[128 * LDH];
-    fs_bf16 w4[16 * LDH];
-    fs_bf16 x[ROWS * LDS];
-    fs_bf16 a1[ROWS * LDH];
-    fs_bf16 a2[ROWS * LDH];
-    fs_bf16 a3[ROWS * LDH];
-    fs_bf16 g1[ROWS * LDH];
-    fs_bf16 g2[ROWS * LDH];
-    fs_bf16 dz4[ROWS * LDS];
-    float z4[ROWS * 16];
+struct TtSmem {
+    alignas(1024) fs_bf16 a1[128 * 128];
+    alignas(128) fs_bf16 a2[128 * 128];
+    alignas(128) fs_bf16 w2[128 * 128];
+    alignas(128) fs_bf16 w3[128 * 128];
+    alignas(128) fs_bf16 w4[16 * 128];
+    alignas(128) fs_bf16 a3[128 * 128];
+    alignas(128) fs_bf16 g[128 * 128];
+    alignas(128) fs_bf16 x[128 * 16];
+    alignas(128) fs_bf16 dz4[128 * 16];
+    alignas(128) fs_bf16 w1[128 * 16];
+    float bias[128 * 3 + 16];
     float db[128 * 3 + 16];
     float loss;
+    alignas(8) unsigned long long mbar;
+    unsigned tmem_base;
+    int give_up;
 };
+// farthest byte a read of a 128-wide tile can reach from the tile's start: 8 K-steps of 16
+// rows (4096 bytes each) plus 15 column blocks and one row block at the larger offset
+#define TT_REACH (7 * 4096 + 15 * 2048 + 256)
+#define TT_SMEM_BYTES \
+    (offsetof(TtSmem, g) + TT_REACH > sizeof(TtSmem) ? offsetof(TtSmem, g) + TT_REACH : sizeof(TtSmem))
 
-__global__ void __launch_bounds__(256) fs_mlp_train_kernel(const float *__restrict__ params,
-                                                           const fs_bf16 *__restrict__ wq, float *__restrict__ grad,
-                                                           const float *__restrict__ xin, const float *__restrict__ zin,
-                                                           int n_rows, int dof, float inv_batch, float *loss_out)
+// column sums over the warp's 32 lanes of v[0..32) (one value per column and lane), added to
+// dst[lane] for lane < ncols; v is consumed
+__device__ __forceinline__ void tt_colsum32(float (&v)[32], float *dst, int lane, int ncols)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    MlpSmem &S = *reinterpret_cast<MlpSmem *>(smem_raw);
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const bool up = (lane & w) != 0;
+#pragma unroll
+        for (int i = 0; i < w; i++) {
+            const float send = up ? v[i] : v[i + w];
+            const float keep = up ? v[i + w] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, w);
+        }
+    }
+    if (lane < ncols) atomicAdd(dst + lane, v[0]);
+}
+
+__global__ void __launch_bounds__(TT_THREADS, 1) fs_mlp_train_tc_kernel(
+    const float *__restrict__ params, const fs_bf16 *__restrict__ wq, float *__restrict__ grad,
+    const float *__restrict__ xin, const float *__restrict__ zin, int n_rows, int dof, float inv_batch,
+    float *loss_out)
+{
+    extern __shared__ __align__(1024) unsigned char tt_raw[];
+    TtSmem &S = *reinterpret_cast<TtSmem *>(tt_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int row0 = blockIdx.x * ROWS;
+    const int n_tiles = (n_rows + 127) / 128;
+    const uint32_t mbar = tc_smem(&S.mbar);
 
-    // ---- stage weights (BF16) and the input tile ----
-    for (int i = tid; i < 128 * 16; i += 256) S.w1[(i / 16) * LDS + i % 16] = wq[Q_W1 + i];
-    for (int i = tid; i < 128 * 128; i += 256) {
-        S.w2[(i / 128) * LDH + i % 128] = wq[Q_W2 + i];
-        S.w3[(i / 128) * LDH + i % 128] = wq[Q_W3 + i];
+    // ---- weights (the BF16 training copy, [out][in]) into canonical tiles, biases ----
+    for (int i = tid; i < 128 * 16; i += TT_THREADS) S.w1[tc_off(i / 16, i % 16, 16)] = wq[Q_W1 + i];
+    for (int i = tid; i < 128 * 128; i += TT_THREADS) {
+        S.w2[tc_off(i / 128, i % 128, 128)] = wq[Q_W2 + i];
+        S.w3[tc_off(i / 128, i % 128, 128)] = wq[Q_W3 + i];
     }
-    for (int i = tid; i < 16 * 128; i += 256) S.w4[(i / 128) * LDH + i % 128] = wq[Q_W4 + i];
-    for (int i = tid; i < ROWS * 16; i += 256) {
-        const int r = i / 16, c = i % 16;
-        const float v = (row0 + r < n_rows) ? xin[(size_t)(row0 + r) * 16 + c] : 0.f;
-        S.x[r * LDS + c] = f2bf(v);
+    for (int i = tid; i < 16 * 128; i += TT_THREADS) S.w4[tc_off(i / 128, i % 128, 128)] = wq[Q_W4 + i];
+    for (int i = tid; i < 128; i += TT_THREADS) {
+        S.bias[i] = params[P_B1 + i];
+        S.bias[128 + i] = params[P_B2 + i];
+        S.bias[256 + i] = params[P_B3 + i];
     }
-    for (int i = tid; i < 128 * 3 + 16; i += 256) S.db[i] = 0.f;
-    if (tid == 0) S.loss = 0.f;
+    if (tid < 16) S.bias[384 + tid] = params[P_B4 + tid];
+    for (int i = tid; i < 128 * 3 + 16; i += TT_THREADS) S.db[i] = 0.f;
+    if (tid == 0) {
+        S.loss = 0.f;
+        S.give_up = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&S.tmem_base)),
+                     "r"(TT_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_async();
+    tc_fence_before();
     __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+    const uint32_t t_row = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's lanes
+    uint32_t phase = 0;
+    bool ok = true, first = true;
 
-    const int wm = warp & 3, wn = warp >> 2;  // 4 row tiles x 2 column halves
-    // ---- forward ----
-    {
-        float acc[1][8][4];
-        zero_acc(acc);
-        warp_gemm<1, 8, false, false>(acc, S.x, LDS, wm * 16, S.w1, LDS, wn * 64, 16, lane);
-        store_relu<8>(acc, params + P_B1, S.a1, wm * 16, wn * 64, lane);
-    }
-    __syncthreads();
-    {
-        float acc[1][8][4];
-        zero_acc(acc);
-        warp_gemm<1, 8, false, false>(acc, S.a1, LDH, wm * 16, S.w2, LDH, wn * 64, 128, lane);
-        store_relu<8>(acc, params + P_B2, S.a2, wm * 16, wn * 64, lane);
-    }
-    __syncthreads();
-    {
-        float acc[1][8][4];
-        zero_acc(acc);
-        warp_gemm<1, 8, false, false>(acc, S.a2, LDH, wm * 16, S.w3, LDH, wn * 64, 128, lane);
-        store_relu<8>(acc, params + P_B3, S.a3, wm * 16, wn * 64, lane);
-    }
-    __syncthreads();
-    if (warp < 4) {
-        float acc[1][2][4];
-        zero_acc(acc);
-        warp_gemm<1, 2, false, false>(acc, S.a3, LDH, warp * 16, S.w4, LDH, 0, 128, lane);
-        const int r = warp * 16 + (lane >> 2), c = (lane & 3) * 2;
-#pragma unroll
-        for (int nt = 0; nt < 2; nt++) {
-            const int col = nt * 8 + c;
-            S.z4[r * 16 + col] = acc[0][nt][0] + params[P_B4 + col];
-            S.z4[r * 16 + col + 1] = acc[0][nt][1] + params[P_B4 + col + 1];
-            S.z4[(r + 8) * 16 + col] = acc[0][nt][2] + params[P_B4 + col];
-            S.z4[(r + 8) * 16 + col + 1] = acc[0][nt][3] + params[P_B4 + col + 1];
+    // one step: the operands made visible to the tensor cores, thread 0 issues the MMAs and
+    // commits, every thread waits (bounded) for them
+    auto step = [&](auto &&issue) {
+        tc_fence_async();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            issue();
+            tc_commit(mbar);
         }
-    }
-    __syncthreads();
-    // ---- loss and its gradient per row ----
-    if (tid < ROWS) {
-        const int r = tid;
-        const bool valid = row0 + r < n_rows;
-        float l = 0.f;
-        float g[16];
+        if (!tc_wait(mbar, phase)) S.give_up = 1;
+        phase ^= 1u;
+        tc_fence_after();
+        __syncthreads();
+        ok = S.give_up == 0;
+        return ok;
+    };
+    // forward epilogue: act = BF16(relu(F + b))
+    auto relu_out = [&](fs_bf16 *act, const float *b) {
+#pragma unroll 1
+        for (int c0 = 0; c0 < 128; c0 += 16) {
+            float v[16];
+            tc_ld16(t_row + TT_F + (uint32_t)c0, v);
 #pragma unroll
-        for (int c = 0; c < 16; c++) g[c] = 0.f;
-        if (valid) {
-            for (int d = 0; d < dof; d++) {
-                const float o = S.z4[r * 16 + d], sr = S.z4[r * 16 + dof + d];
-                const float th = tanhf(0.25f * sr);
-                const float s = 4.f * th;
-                const float e = expf(-s);
-                const float z = zin[(size_t)(row0 + r) * 8 + d];
-                const float df = z - o;
-                l += 0.5f * df * df * e + 0.5f * s;
-                g[d] = -df * e * inv_batch;
-                g[dof + d] = (0.5f - 0.5f * df * df * e) * (1.f - th * th) * inv_batch;
+            for (int i = 0; i < 16; i++) v[i] = fmaxf(v[i] + b[c0 + i], 0.f);
+            tc_st8(act + tc_off(tid, c0, 128), v);
+            tc_st8(act + tc_off(tid, c0 + 8, 128), v + 8);
+        }
+    };
+    // backward epilogue: dZ = F * (act > 0) -> g as BF16, its FP32 column sums into dbl
+    auto grad_out = [&](const fs_bf16 *act, float *dbl) {
+#pragma unroll 1
+        for (int c0 = 0; c0 < 128; c0 += 32) {
+            float v[32];
+            tc_ld16(t_row + TT_F + (uint32_t)c0, *reinterpret_cast<float(*)[16]>(v));
+            tc_ld16(t_row + TT_F + (uint32_t)c0 + 16u, *reinterpret_cast<float(*)[16]>(v + 16));
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint4 u = *reinterpret_cast<const uint4 *>(act + tc_off(tid, c0 + 8 * q, 128));
+                const unsigned w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    if (!(__uint_as_float(w[e] << 16) > 0.f)) v[8 * q + 2 * e] = 0.f;
+                    if (!(__uint_as_float(w[e] & 0xFFFF0000u) > 0.f)) v[8 * q + 2 * e + 1] = 0.f;
+                }
+                tc_st8(S.g + tc_off(tid, c0 + 8 * q, 128), v + 8 * q);
             }
+            tt_colsum32(v, dbl + c0, lane, 32);
         }
+    };
+
+    for (int tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+        const int row = tile * 128 + tid;
+        const bool valid = row < n_rows;
+        {
+            float h[16];
 #pragma unroll
-        for (int c = 0; c < 16; c++) {
-            S.dz4[r * LDS + c] = f2bf(g[c]);
-            atomicAdd(&S.db[384 + c], g[c]);
+            for (int c = 0; c < 16; c++) h[c] = valid ? xin[(size_t)row * 16 + c] : 0.f;
+            tc_st8(S.x + tc_off(tid, 0, 16), h);
+            tc_st8(S.x + tc_off(tid, 8, 16), h + 8);
         }
-        atomicAdd(&S.loss, l);
+        // ---- forward ----
+        if (!step([&] { tc_mma(tmem + TT_F, tc_desc(S.x, 16), tc_desc(S.w1, 16), tc_idesc(128, 128), 0); }))
+            break;
+        relu_out(S.a1, S.bias);
+        if (!step([&] {
+                for (int kk = 0; kk < 8; kk++)
+                    tc_mma(tmem + TT_F, tc_desc(S.a1 + kk * 128, 128), tc_desc(S.w2 + kk * 128, 128),
+                           tc_idesc(128, 128), kk > 0);
+            }))
+            break;
+        relu_out(S.a2, S.bias + 128);
+        if (!step([&] {
+                for (int kk = 0; kk < 8; kk++)
+                    tc_mma(tmem + TT_F, tc_desc(S.a2 + kk * 128, 128), tc_desc(S.w3 + kk * 128, 128),
+                           tc_idesc(128, 128), kk > 0);
+            }))
+            break;
+        relu_out(S.a3, S.bias + 256);
+        if (!step([&] {
+                for (int kk = 0; kk < 8; kk++)
+                    tc_mma(tmem + TT_F, tc_desc(S.a3 + kk * 128, 128), tc_desc(S.w4 + kk * 128, 128),
+                           tc_idesc(128, 16), kk > 0);
+            }))
+            break;
+        // ---- loss and its gradient for this thread's row ----
+        {
+            float z4[16], g[32];
+            tc_ld16(t_row + TT_F, z4);
+#pragma unroll
+            for (int c = 0; c < 16; c++) z4[c] += S.bias[384 + c];
+#pragma unroll
+            for (int c = 0; c < 32; c++) g[c] = 0.f;
+            float l = 0.f;
+            if (valid) {
+#pragma unroll
+                for (int d = 0; d < 8; d++) {
+                    if (d >= dof) break;
+                    float sr = 0.f;
+#pragma unroll
+                    for (int c = 0; c < 16; c++) sr = c == dof + d ? z4[c] : sr;
+                    const float o = z4[d];
+                    const float th = tanhf(0.25f * sr);
+                    const float s = 4.f * th;
+                    const float e = expf(-s);
+                    const float z = zin[(size_t)row * 8 + d];
+                    const float df = z - o;
+                    l += 0.5f * df * df * e + 0.5f * s;
+                    g[d] = -df * e * inv_batch;
+                    const float gs = (0.5f - 0.5f * df * df * e) * (1.f - th * th) * inv_batch;
+#pragma unroll
+                    for (int c = 0; c < 16; c++) g[c] = c == dof + d ? gs : g[c];
+                }
+            }
+            tc_st8(S.dz4 + tc_off(tid, 0, 16), g);
+            tc_st8(S.dz4 + tc_off(tid, 8, 16), g + 8);
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) l += __shfl_xor_sync(0xFFFFFFFFu, l, off);
+            if (lane == 0) atomicAdd(&S.loss, l);
+            tt_colsum32(g, S.db + 384, lane, 16);
+        }
+        // ---- backward ----
+        const uint32_t acc0 = first ? 0u : 1u;
+        if (!step([&] {
+                for (int kk = 0; kk < 8; kk++)  // dW4^T += A3^T dZ4 (M = inputs, N = outputs)
+                    tc_mma(tmem + TT_DW4, tc_desc_mn(S.a3 + kk * 2048, 128), tc_desc_mn(S.dz4 + kk * 256, 16),
+                           tc_idesc(128, 16, true, true), acc0 | (kk > 0));
+                // dA3 = dZ4 W4
+                tc_mma(tmem + TT_F, tc_desc(S.dz4, 16), tc_desc_mn(S.w4, 128), tc_idesc(128, 128, false, true), 0);
+            }))
+            break;
+        grad_out(S.a3, S.db + 256);
+        if (!step([&] {
+                for (int kk = 0; kk < 8; kk++)  // dW3 += dZ3^T A2
+                    tc_mma(tmem + TT_DW3, tc_desc_mn(S.g + kk * 2048, 128), tc_desc_mn(S.a2 + kk * 2048, 128),
+                           tc_idesc(128, 128, true, true), acc0 | (kk > 0));
+                for (int kk = 0; kk < 8; kk++)  // dA2 = dZ3 W3
+                    tc_mma(tmem + TT_F, tc_desc(S.g + kk * 128, 128), tc_desc_mn(S.w3 + kk * 2048, 128),
+                           tc_idesc(128, 128, false, true), kk > 0);
+            }))
+            break;
+        grad_out(S.a2, S.db + 128);
+        if (!step([&] {
+                for (int kk = 0; kk < 8; kk++)  // dW2 += dZ2^T A1
+                    tc_mma(tmem + TT_DW2, tc_desc_mn(S.g + kk * 2048, 128), tc_desc_mn(S.a1 + kk * 2048, 128),
+                           tc_idesc(128, 128, true, true), acc0 | (kk > 0));
+                for (int kk = 0; kk < 8; kk++)  // dA1 = dZ2 W2
+                    tc_mma(tmem + TT_F, tc_desc(S.g + kk * 128, 128), tc_desc_mn(S.w2 + kk * 2048, 128),
+                           tc_idesc(128, 128, false, true), kk > 0);
+            }))
+            break;
+        grad_out(S.a1, S.db);
+        if (!step([&] {
+                for (int kk = 0; kk < 8; kk++)  // dW1 += dZ1^T X
+                    tc_mma(tmem + TT_DW1, tc_desc_mn(S.g + kk * 2048, 128), tc_desc_mn(S.x + kk * 256, 16),
+                           tc_idesc(128, 16, true, true), acc0 | (kk > 0));
+            }))
+            break;
+        first = false;
     }
+    if (ok && !first) {
+        // the CTA's weight gradients out of tensor memory: thread t = lane t is output row t
+        // of dW1..dW3 and input column t of dW4
+#pragma unroll 1
+        for (int c0 = 0; c0 < 128; c0 += 16) {
+            float v[16];
+            tc_ld16(t_row + TT_DW2 + (uint32_t)c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; i++) atomicAdd(grad + P_W2 + tid * 128 + c0 + i, v[i]);
+            tc_ld16(t_row + TT_DW3 + (uint32_t)c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; i++) atomicAdd(grad + P_W3 + tid * 128 + c0 + i, v[i]);
+        }
+        {
+            float v[16];
+            tc_ld16(t_row + TT_DW1, v);
+#pragma unroll
+            for (int i = 0; i < 16; i++) atomicAdd(grad + P_W1 + tid * 16 + i, v[i]);
+            tc_ld16(t_row + TT_DW4, v);
+#pragma unroll
+            for (int o = 0; o < 16; o++) atomicAdd(grad + P_W4 + o * 128 + tid, v[o]);
+        }
+        for (int i = tid; i < 128; i += TT_THREADS) {
+            atomicAdd(grad + P_B1 + i, S.db[i]);
+            atomicAdd(grad + P_B2 + i, S.db[128 + i]);
+            atomicAdd(grad + P_B3 + i, S.db[256 + i]);
+        }
+        if (tid < 16) atomicAdd(grad + P_B4 + tid, S.db[384 + tid]);
+        if (tid == 0 && loss_out) atomicAdd(loss_out, S.loss);
+    }
+    if (!ok && tid == 0 && loss_out) atomicAdd(loss_out, __int_as_float(0x7FC00000));  // gave up: NaN loss
+    // release the tensor memory once no MMA is in flight: after a give-up, wait (bounded)
+    // for the last commit's phase before freeing the columns
+    if (!ok) tc_wait(mbar, phase ^ 1u);
+    tc_fence_before();
     __syncthreads();
-    // ---- backward ----
-    {   // dW4 += dZ4^T A3: [16 x 128]
-        float acc[1][2][4];
-        zero_acc(acc);
-        warp_gemm<1, 2, true, true>(acc, S.dz4, LDS, 0, S.a3, LDH, warp * 16, ROWS, lane);
-        add_dw<1, 2>(acc, grad + P_W4, 128, 0, warp * 16, lane);
-    }
-    {   // dA3 = dZ4 W4 -> dZ3 (g1)
-        float acc[1][8][4];
-        zero_acc(acc);
-        warp_gemm<1, 8, false, true>(acc, S.dz4, LDS, wm * 16, S.w4, LDH, wn * 64, 16, lane);
-        store_dz<8>(acc, S.a3, S.g1, S.db + 256, wm * 16, wn * 64, lane);
-    }
-    __syncthreads();
-    {   // dW3 += dZ3^T A2
-        float acc[2][8][4];
-        zero_acc(acc);
-        warp_gemm<2, 8, true, true>(acc, S.g1, LDH, wm * 32, S.a2, LDH, wn * 64, ROWS, lane);
-        add_dw<2, 8>(acc, grad + P_W3, 128, wm * 32, wn * 64, lane);
-    }
-    {   // dA2 = dZ3 W3 -> dZ2 (g2)
-        float acc[1][8][4];
-        zero_acc(acc);
-        warp_gemm<1, 8, false, true>(acc, S.g1, LDH, wm * 16, S.w3, LDH, wn * 64, 128, lane);
-        store_dz<8>(acc, S.a2, S.g2, S.db + 128, wm * 16, wn * 64, lane);
-    }
-    __syncthreads();
-    {   // dW2 += dZ2^T A1
-        float acc[2][8][4];
-        zero_acc(acc);
-        warp_gemm<2, 8, true, true>(acc, S.g2, LDH, wm * 32, S.a1, LDH, wn * 64, ROWS, lane);
-        add_dw<2, 8>(acc, grad + P_W2, 128, wm * 32, wn * 64, lane);
-    }
-    __syncthreads();  // g1 is rewritten next
-    {   // dA1 = dZ2 W2 -> dZ1 (g1)
-        float acc[1][8][4];
-        zero_acc(acc);
-        warp_gemm<1, 8, false, true>(acc, S.g2, LDH, wm * 16, S.w2, LDH, wn * 64, 128, lane);
-        store_dz<8>(acc, S.a1, S.g1, S.db, wm * 16, wn * 64, lane);
-    }
-    __syncthreads();
-    {   // dW1 += dZ1^T X: [128 x 16]
-        float acc[1][2][4];
-        zero_acc(acc);
-        warp_gemm<1, 2, true, true>(acc, S.g1, LDH, warp * 16, S.x, LDS, 0, ROWS, lane);
-        add_dw<1, 2>(acc, grad + P_W1, 16, warp * 16, 0, lane);
-    }
-    __syncthreads();
-    for (int i = tid; i < 128; i += 256) {
-        atomicAdd(grad + P_B1 + i, S.db[i]);
-        atomicAdd(grad + P_B2 + i, S.db[128 + i]);
-        atomicAdd(grad + P_B3 + i, S.db[256 + i]);
-    }
-    if (tid < 16) atomicAdd(grad + P_B4 + tid, S.db[384 + tid]);
-    if (tid == 0 && loss_out) atomicAdd(loss_out, S.loss);
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TT_TMEM_COLS)
+                     : "memory");
 }
 
 // Adam step on the FP32 master weights; writes the BF16 training copy and clears the
@@ -430,16 +445,20 @@ extern "C" int fs_mlp_train_step(const float *params, const uint16_t *wq, float 
 {
     if (dof < 1 || dof > 8 || n_rows < 1)
         return fsi_thread_error(FS_ERR_CONFIG, "fs_mlp_train_step: need 1 <= dof <= 8 and n_rows >= 1");
-    static bool attr_done = false;
-    if (!attr_done) {
-        cudaError_t e = cudaFuncSetAttribute(fs_mlp_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)sizeof(MlpSmem));
+    static int sms = 0;
+    if (!sms) {
+        cudaError_t e = cudaFuncSetAttribute(fs_mlp_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)TT_SMEM_BYTES);
         if (e != cudaSuccess) return fsi_thread_error(FS_ERR_CUDA, cudaGetErrorString(e));
-        attr_done = true;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms < 1) sms = 1;
     }
-    fs_mlp_train_kernel<<<(n_rows + ROWS - 1) / ROWS, 256, sizeof(MlpSmem), (cudaStream_t)stream>>>(
+    const int n_tiles = (n_rows + 127) / 128;
+    fs_mlp_train_tc_kernel<<<n_tiles < sms ? n_tiles : sms, TT_THREADS, TT_SMEM_BYTES, (cudaStream_t)stream>>>(
         params, (const fs_bf16 *)wq, grad, x, z, n_rows, dof, inv_batch, loss);
-    return launch_check("fs_mlp_train_kernel");
+    return launch_check("fs_mlp_train_tc_kernel");
 }
 
 extern "C" int fs_mlp_adam(float *params, float *m, float *v, float *grad, uint16_t *wq, int32_t step, float lr,
