@@ -30,6 +30,7 @@
 #define P_B3 (P_W3 + 128 * 128)
 #define P_W4 (P_B3 + 128)
 #define P_B4 (P_W4 + 16 * 128)
+static_assert(P_W1 % 4 == 0 && P_W2 % 4 == 0 && P_W3 % 4 == 0, "16-byte gradient rows");
 
 // BF16 weight copy used by training (row-major, same order as the FP32 weights, no biases)
 #define Q_W1 0
@@ -121,13 +122,19 @@ __global__ void __launch_bounds__(TT_THREADS, 1) fs_mlp_train_tc_kernel(
     const int n_tiles = (n_rows + 127) / 128;
     const uint32_t mbar = tc_smem(&S.mbar);
 
-    // ---- weights (the BF16 training copy, [out][in]) into canonical tiles, biases ----
-    for (int i = tid; i < 128 * 16; i += TT_THREADS) S.w1[tc_off(i / 16, i % 16, 16)] = wq[Q_W1 + i];
-    for (int i = tid; i < 128 * 128; i += TT_THREADS) {
-        S.w2[tc_off(i / 128, i % 128, 128)] = wq[Q_W2 + i];
-        S.w3[tc_off(i / 128, i % 128, 128)] = wq[Q_W3 + i];
+    // ---- weights (the BF16 training copy, [out][in]) into canonical tiles, eight
+    // consecutive inputs (one core-matrix row, 16 bytes) per load and store; biases ----
+    {
+        const uint4 *q = reinterpret_cast<const uint4 *>(wq);
+        for (int i = tid; i < 128 * 16 / 8; i += TT_THREADS)
+            *reinterpret_cast<uint4 *>(S.w1 + tc_off(i / 2, (i % 2) * 8, 16)) = q[Q_W1 / 8 + i];
+        for (int i = tid; i < 128 * 128 / 8; i += TT_THREADS) {
+            *reinterpret_cast<uint4 *>(S.w2 + tc_off(i / 16, (i % 16) * 8, 128)) = q[Q_W2 / 8 + i];
+            *reinterpret_cast<uint4 *>(S.w3 + tc_off(i / 16, (i % 16) * 8, 128)) = q[Q_W3 / 8 + i];
+        }
+        for (int i = tid; i < 16 * 128 / 8; i += TT_THREADS)
+            *reinterpret_cast<uint4 *>(S.w4 + tc_off(i / 16, (i % 16) * 8, 128)) = q[Q_W4 / 8 + i];
     }
-    for (int i = tid; i < 16 * 128; i += TT_THREADS) S.w4[tc_off(i / 128, i % 128, 128)] = wq[Q_W4 + i];
     for (int i = tid; i < 128; i += TT_THREADS) {
         S.bias[i] = params[P_B1 + i];
         S.bias[128 + i] = params[P_B2 + i];
@@ -213,8 +220,15 @@ __global__ void __launch_bounds__(TT_THREADS, 1) fs_mlp_train_tc_kernel(
         const bool valid = row < n_rows;
         {
             float h[16];
+            const float4 *xr = reinterpret_cast<const float4 *>(xin + (size_t)row * 16);
 #pragma unroll
-            for (int c = 0; c < 16; c++) h[c] = valid ? xin[(size_t)row * 16 + c] : 0.f;
+            for (int c = 0; c < 4; c++) {
+                const float4 f = valid ? xr[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+                h[4 * c] = f.x;
+                h[4 * c + 1] = f.y;
+                h[4 * c + 2] = f.z;
+                h[4 * c + 3] = f.w;
+            }
             tc_st8(S.x + tc_off(tid, 0, 16), h);
             tc_st8(S.x + tc_off(tid, 8, 16), h + 8);
         }
@@ -320,21 +334,25 @@ __global__ void __launch_bounds__(TT_THREADS, 1) fs_mlp_train_tc_kernel(
     if (ok && !first) {
         // the CTA's weight gradients out of tensor memory: thread t = lane t is output row t
         // of dW1..dW3 and input column t of dW4
+        // (16-byte vector atomics: the parameter offsets of W1..W3 are multiples of 4 floats)
+        auto add4 = [](float *dst, const float *v) {
+            atomicAdd(reinterpret_cast<float4 *>(dst), make_float4(v[0], v[1], v[2], v[3]));
+        };
 #pragma unroll 1
         for (int c0 = 0; c0 < 128; c0 += 16) {
             float v[16];
             tc_ld16(t_row + TT_DW2 + (uint32_t)c0, v);
 #pragma unroll
-            for (int i = 0; i < 16; i++) atomicAdd(grad + P_W2 + tid * 128 + c0 + i, v[i]);
+            for (int i = 0; i < 16; i += 4) add4(grad + P_W2 + tid * 128 + c0 + i, v + i);
             tc_ld16(t_row + TT_DW3 + (uint32_t)c0, v);
 #pragma unroll
-            for (int i = 0; i < 16; i++) atomicAdd(grad + P_W3 + tid * 128 + c0 + i, v[i]);
+            for (int i = 0; i < 16; i += 4) add4(grad + P_W3 + tid * 128 + c0 + i, v + i);
         }
         {
             float v[16];
             tc_ld16(t_row + TT_DW1, v);
 #pragma unroll
-            for (int i = 0; i < 16; i++) atomicAdd(grad + P_W1 + tid * 16 + i, v[i]);
+            for (int i = 0; i < 16; i += 4) add4(grad + P_W1 + tid * 16 + i, v + i);
             tc_ld16(t_row + TT_DW4, v);
 #pragma unroll
             for (int o = 0; o < 16; o++) atomicAdd(grad + P_W4 + o * 128 + tid, v[o]);
@@ -445,6 +463,8 @@ extern "C" int fs_mlp_train_step(const float *params, const uint16_t *wq, float 
 {
     if (dof < 1 || dof > 8 || n_rows < 1)
         return fsi_thread_error(FS_ERR_CONFIG, "fs_mlp_train_step: need 1 <= dof <= 8 and n_rows >= 1");
+    if (((uintptr_t)wq | (uintptr_t)x | (uintptr_t)grad) & 15u)
+        return fsi_thread_error(FS_ERR_CONFIG, "fs_mlp_train_step: wq, x and grad must be 16-byte aligned");
     static int sms = 0;
     if (!sms) {
         cudaError_t e = cudaFuncSetAttribute(fs_mlp_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -299,7 +299,8 @@ int fs_mlp_sizes(int64_t *n_param, int64_t *n_bf16, int64_t *n_frag_u2, int64_t 
 /* One forward + backward pass over n_rows (features x[n][16], targets z[n][8]) adding the
  * gradient of the mean loss (inv_batch = 1/batch) to grad and the loss sum to *loss; on the
  * tcgen05 tensor cores (one CTA per SM, 222 KB of shared memory and all 512 tensor-memory
- * columns each).  A CTA whose bounded wait on its MMAs gives up adds NaN to *loss. */
+ * columns each).  wq, x and grad must be 16-byte aligned.  A CTA whose bounded wait on its
+ * MMAs gives up adds NaN to *loss. */
 int fs_mlp_train_step(const float *params, const uint16_t *wq, float *grad, const float *x,
                       const float *z, int32_t n_rows, int32_t dof, float inv_batch, float *loss,
                       void *stream);
