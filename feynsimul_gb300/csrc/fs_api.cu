@@ -69,7 +69,6 @@ struct fs_handle {
     int cor_ilv = 0;  // correlator lags summed in one slice pass over a doubled slice buffer
     int pipe = 0;     // correlator helpers one measurement behind the movers (FS_PIPE)
     long long snstride = 0;  // FS_PIPE: one path snapshot in shared memory, elements
-    int psets = 1;           // FS_PIPE: helper sets taking the measurements in turn (FS_PSETS)
     int mx = 1;       // thread groups per CTA: 1 moving + mx - 1 summing correlator lags (FS_MX)
     long long cwstride = 0;  // per-walker correlator buffer in shared memory, elements
     int resident_per_sm = 0;  // resident CTAs per SM of the sweep kernel (fs_run_host), 0 = not yet queried
@@ -327,8 +326,7 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n#define FS_GLOBAL " << (c.global_path ? 1 : 0)
       << "\n#define FS_VCACHE " << (h.vstride ? 1 : 0) << "\n#define FS_VSTRIDE " << h.vstride
       << "\n#define FS_COR_ILV " << h.cor_ilv << "\n#define FS_CWSTRIDE " << h.cwstride << "\n#define FS_MX "
-      << h.mx << "\n#define FS_PIPE " << h.pipe << "\n#define FS_PSETS " << h.psets << "\n#define FS_SNSTRIDE "
-      << h.snstride << "\n";
+      << h.mx << "\n#define FS_PIPE " << h.pipe << "\n#define FS_SNSTRIDE " << h.snstride << "\n";
     {
         const int mv = c.moves ? c.moves : FS_MOVE_BISECTION;
         const double nb = (double)c.n_slices / c.beta;
@@ -650,8 +648,7 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
         // moves.
         // The pipelined helpers give each pair of threads 4 consecutive lags (N/4 lag threads
         // per walker, in pairs of one walker: an even number of segment threads) and sum
-        // FP32 partials over the doubled slice values.  With at most 4 correlators (running
-        // sums in registers) two helper sets take the measurements in turn (FS_PSETS = 2).
+        // FP32 partials over the doubled slice values.
         if (!h->cors.empty() && c.enable_parallelize_path && !c.global_path && !c.learned && h->tpw <= 32) {
             const int lag_threads = std::min(c.n_slices / 2, 64);
             const int wpw = 32 / h->tpw;
@@ -659,25 +656,23 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
             const int groups = (c.n_slices / 4 + h->tpw - 1) / h->tpw;
             const bool fma_partials = (c.accum == FS_ACCUM_FP64 || c.accum == FS_ACCUM_KAHAN) &&
                                       !c.enable_double && c.partials == FS_PARTIALS_FP32;
-            const int sets = h->cors.size() <= 4 ? 2 : 1;
             if (fma_partials && c.n_slices % 8 == 0 && c.n_slices >= 16 && h->tpw >= 2 && c.n_walkers % wpw == 0 &&
                 wpb_min % wpw == 0 && c.n_walkers % wpb_min == 0 &&
-                (long long)wpb_min * h->tpw * (1 + sets * groups) <= 512) {
+                (long long)wpb_min * h->tpw * (1 + groups) <= 512) {
                 h->pipe = 1;
-                h->psets = sets;
-                h->mx = 1 + sets * groups;
+                h->mx = 1 + groups;
             } else if (lag_threads > h->tpw) {
                 h->mx = lag_threads / h->tpw;
             }
-            if (c.walkers_per_block > 0 && c.n_walkers % c.walkers_per_block) h->mx = 1, h->pipe = 0, h->psets = 1;
+            if (c.walkers_per_block > 0 && c.n_walkers % c.walkers_per_block) h->mx = 1, h->pipe = 0;
         }
-        const long long lag_tpw = (long long)h->tpw * (h->pipe ? (h->mx - 1) / h->psets : h->mx);
+        const long long lag_tpw = (long long)h->tpw * (h->mx - h->pipe);
         const long long lpt = h->pipe ? 4 : (c.n_slices / 2 + lag_tpw - 1) / lag_tpw;
         h->cor_ilv = (c.accum != 0 && !c.enable_double && lpt <= 4) ? 1 : 0;
         // per-walker stride an odd multiple of 64 bytes: two walkers sharing a warp read
         // opposite bank halves
         const long long q = 64 / (long long)h->ft;
-        long long cw = (long long)h->cors.size() * c.n_slices * (h->cor_ilv ? 2 : 1) * h->psets;
+        long long cw = (long long)h->cors.size() * c.n_slices * (h->cor_ilv ? 2 : 1);
         if (h->pipe) {
             // two path snapshots in the padded slice layout, 16-word multiples (FS_SNSTRIDE)
             const long long dstr = c.n_slices + (c.n_slices >> c.bisection_level);

@@ -35,13 +35,6 @@
 // m + 1.  One CTA barrier per measurement hands a snapshot over; the movers sync among
 // themselves on named barrier 1 and the helpers on named barrier 2.  Every sum is formed in
 // the same order as without the pipeline, so the results are the same bit for bit.
-// FS_PSETS = 2: two helper sets take the measurements in turn (set m mod 2), so each has two
-// sweeps for one measurement.  Snapshot m mod 2 is handed over by named barriers: the movers
-// wait on EMPTY (4 + 2 set) before writing it and arrive on FULL (3 + 2 set) after; the set
-// waits on FULL, reads the snapshot into its own correlator values, arrives on EMPTY, and
-// syncs on its own barrier 7 + set before its lag sums.  Each set keeps FP64 running sums of
-// its measurements and set 1's are added to set 0's at the end, so the correlator sums equal
-// the sequential ones up to the order of the FP64 additions.
 #ifndef FS_MX
 #define FS_MX 1
 #endif
@@ -51,14 +44,9 @@
 #ifndef FS_SNSTRIDE
 #define FS_SNSTRIDE 0
 #endif
-#ifndef FS_PSETS
-#define FS_PSETS 1
-#endif
 #define FS_MBLOCK (FS_WPB * FS_TPW)          // threads that run the moves
 #define FS_BLOCK (FS_MBLOCK * FS_MX)
-#define FS_HGROUPS (FS_PIPE ? (FS_MX - 1) / FS_PSETS : FS_MX)  // thread groups per helper set
-#define FS_HBLOCK (FS_MBLOCK * FS_HGROUPS)   // threads of one helper set
-#define FS_CTPW (FS_TPW * FS_HGROUPS)        // correlator threads per walker (per helper set)
+#define FS_CTPW (FS_TPW * (FS_MX - FS_PIPE))  // correlator threads per walker
 #if FS_PIPE
 #define FS_LPT 4                             // lags 2 lt .. 2 lt + 3 (even lt)
 #define FS_LAG(j) (2 * lt + (j))
@@ -72,13 +60,7 @@
 #if FS_PIPE && (FS_MX < 2 || FS_MBLOCK % 32 != 0 || FS_LEARNED || FS_SNSTRIDE < FS_DOF * (FS_N + (FS_N >> FS_S)) || FS_SNSTRIDE % 16 != 0 || FS_N % 8 != 0 || FS_CTPW < FS_N / 4 || FS_TPW % 2 != 0)
 #error "pipelined correlator helpers need helper groups, whole warps of movers and a path snapshot"
 #endif
-#if FS_PSETS != 1 && !(FS_PSETS == 2 && FS_PIPE && (FS_MX - 1) % 2 == 0)
-#error "two helper sets need the pipelined helpers and an even number of helper groups"
-#endif
 #define FS_COR_REGS (FS_ACCUM != 3 && FS_LPT * FS_NCOR <= 16)
-#if FS_PSETS == 2 && !FS_COR_REGS
-#error "two helper sets keep their running sums in registers"
-#endif
 #define FS_CSTEP (FS_N % 4 == 0 ? 4 : 1)  // FP64 correlator: partial sums over s1 mod 4
 // Correlator FP64 sums of FP32 builds (FP64, Kahan and study modes): one measurement's
 // products of a lag are summed in FP32, then added to the lag's FP64 running sum.  The FP32
@@ -115,7 +97,7 @@
 #ifndef FS_CWSTRIDE
 #define FS_CWSTRIDE (FS_NCOR * FS_CSTRIDE)  // per-walker correlator buffer (the host pads it)
 #endif
-#if FS_CWSTRIDE < 2 * FS_SNSTRIDE + FS_PSETS * FS_NCOR * FS_CSTRIDE
+#if FS_CWSTRIDE < 2 * FS_SNSTRIDE + FS_NCOR * FS_CSTRIDE
 #error "per-walker correlator buffer smaller than its slice values"
 #endif
 
@@ -526,16 +508,6 @@ __device__ __forceinline__ double fs_f2d(float x)
 }
 __device__ __forceinline__ double fs_f2d(double x) { return x; }
 
-// named barriers with a thread count (whole warps): wait for the phase, or only arrive
-__device__ __forceinline__ void fs_bar_sync(int id, int count)
-{
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-__device__ __forceinline__ void fs_bar_arrive(int id, int count)
-{
-    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-
 // float-float accumulation: Knuth's TwoSum yields the exact rounding error of s + q, and the
 // errors are summed on the side (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM
 // J. Sci. Comput. 26 (2005), Algorithm 4.4 "Sum2"); s + e then carries about 48 significant
@@ -654,10 +626,8 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     const int t = tid_b % FS_TPW;
     const bool mover = FS_MX == 1 || grp == 0;
     // this thread's lags FS_LAG(j): lt + j * FS_CTPW; with FS_PIPE the even helper lanes
-    // lt < N/4 of each helper set hs own lags 2 lt + j
-    const int hgrp = grp - FS_PIPE;                // helper group (-1: movers)
-    const int hs = FS_PIPE && !mover ? hgrp / FS_HGROUPS : 0;
-    const int lt = (FS_PIPE && !mover ? hgrp % FS_HGROUPS : hgrp) * FS_TPW + t;
+    // lt < N/4 own lags 2 lt + j
+    const int lt = (grp - FS_PIPE) * FS_TPW + t;
     const bool lagger = FS_PIPE ? !mover && lt < FS_N / 4 && (lt & 1) == 0 : true;
     const int w0 = (blockIdx.x + a.block_offset) * FS_WPB;
     const int w = w0 + wl;
@@ -776,8 +746,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #if FS_NCOR > 0
         FsCorAcc *g_cor = (FsCorAcc *)a.cor_means + (size_t)w * FS_NCOR * FS_HALF_N;
         // FS_PIPE: two path snapshots ahead of the correlator values
-        // one measurement's values (each helper set its own)
-        FT *const C = s_cor + wl * FS_CWSTRIDE + 2 * FS_SNSTRIDE + hs * (FS_NCOR * FS_CSTRIDE);
+        FT *const C = s_cor + wl * FS_CWSTRIDE + 2 * FS_SNSTRIDE;  // one measurement's values
 #if FS_PIPE
         FT *const SN0 = s_cor + wl * FS_CWSTRIDE;
         FT *SN = SN0;  // the movers' next snapshot
@@ -789,7 +758,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #pragma unroll
             for (int j = 0; j < FS_LPT; j++) {
                 const int tau = FS_LAG(j);
-                cacc[c][j] = lagger && hs == 0 && tau < FS_HALF_N ? g_cor[c * FS_HALF_N + tau] : (FsCorAcc)0;
+                cacc[c][j] = lagger && tau < FS_HALF_N ? g_cor[c * FS_HALF_N + tau] : (FsCorAcc)0;
             }
 #endif
 #endif
@@ -1140,19 +1109,6 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         if (!mover) {
             // helpers: measurement run on its snapshot while the movers sweep towards the
             // next one
-#if FS_PSETS == 2
-#pragma unroll 1
-            for (int run = hs; run < FS_OPRUNS; run += 2) {
-                fs_bar_sync(3 + 2 * hs, FS_MBLOCK + FS_HBLOCK);    // snapshot run written
-                const FT *Q = SN0 + hs * FS_SNSTRIDE;
-#pragma unroll 1
-                for (int s = lt; s < FS_N; s += FS_CTPW) fs_cor_put(Q, s);
-                __threadfence_block();
-                fs_bar_arrive(4 + 2 * hs, FS_MBLOCK + FS_HBLOCK);  // snapshot read
-                fs_bar_sync(7 + hs, FS_HBLOCK);                     // the set's values written
-                fs_cor_lags4(C);
-            }
-#else
 #pragma unroll 1
             for (int run = 0; run < FS_OPRUNS; run++) {
                 __syncthreads();
@@ -1162,7 +1118,6 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
                 asm volatile("bar.sync 2, %0;" ::"n"(FS_BLOCK - FS_MBLOCK) : "memory");
                 fs_cor_lags4(C);
             }
-#endif
         } else
 #endif
         {
@@ -1246,10 +1201,6 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #else
             const int s_lo = 0, s_hi = FS_N;
 #endif
-#if FS_PIPE && FS_PSETS == 2
-            // snapshot run mod 2 free again: its helper set has read measurement run - 2
-            if (run >= 2) fs_bar_sync(4 + 2 * (run & 1), FS_MBLOCK + FS_HBLOCK);
-#endif
 #pragma unroll 1
             for (int s = s_lo; s < (mover ? s_hi : s_lo); s++) {
 #if FS_NOPS > 0
@@ -1293,12 +1244,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             if (mover) fs_op_flush();
 #endif
 #if FS_PIPE
-#if FS_PSETS == 2
-            __threadfence_block();
-            fs_bar_arrive(3 + 2 * (run & 1), FS_MBLOCK + FS_HBLOCK);  // the snapshot to set run mod 2
-#else
             __syncthreads();  // the snapshot goes to the helper threads
-#endif
             SN = SN == SN0 ? SN0 + FS_SNSTRIDE : SN0;
 #elif FS_NCOR > 0
             FS_WSYNC();
@@ -1306,12 +1252,6 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #endif
             FS_WSYNC();
         }
-#if FS_PIPE && FS_PSETS == 2
-        // the last two snapshots read (every EMPTY arrival of the helpers met by one wait)
-#pragma unroll 1
-        for (int m = FS_OPRUNS >= 2 ? FS_OPRUNS - 2 : 0; m < FS_OPRUNS; m++)
-            fs_bar_sync(4 + 2 * (m & 1), FS_MBLOCK + FS_HBLOCK);
-#endif
         }
 
         // ---- epilogue (kernel.c:801-836) ----
@@ -1334,33 +1274,12 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
         }
 #endif
 #if FS_NCOR > 0 && FS_COR_REGS
-#if FS_PSETS == 2
-        {
-            // set 1's running sums (in its correlator values' buffer, free now) added to set 0's
-            double *xs = reinterpret_cast<double *>(s_cor + wl * FS_CWSTRIDE + 2 * FS_SNSTRIDE +
-                                                    FS_NCOR * FS_CSTRIDE);
-            __syncthreads();  // every lag sum of set 1 done with its correlator values
-            if (lagger && hs == 1)
-#pragma unroll
-                for (int c = 0; c < FS_NCOR; c++)
-#pragma unroll
-                    for (int j = 0; j < FS_LPT; j++)
-                        if (FS_LAG(j) < FS_HALF_N) xs[c * FS_HALF_N + FS_LAG(j)] = cacc[c][j];
-            __syncthreads();
-            if (lagger && hs == 0)
-#pragma unroll
-                for (int c = 0; c < FS_NCOR; c++)
-#pragma unroll
-                    for (int j = 0; j < FS_LPT; j++)
-                        if (FS_LAG(j) < FS_HALF_N) cacc[c][j] = __dadd_rn(cacc[c][j], xs[c * FS_HALF_N + FS_LAG(j)]);
-        }
-#endif
 #pragma unroll
         for (int c = 0; c < FS_NCOR; c++)
 #pragma unroll
             for (int j = 0; j < FS_LPT; j++) {
                 const int tau = FS_LAG(j);
-                if (lagger && hs == 0 && tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = cacc[c][j];
+                if (lagger && tau < FS_HALF_N) g_cor[c * FS_HALF_N + tau] = cacc[c][j];
             }
 #endif
 #if FS_GLOBAL

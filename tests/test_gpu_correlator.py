@@ -76,20 +76,17 @@ def test_fp32_partials_within_bound_of_float_float(parallel, N, S, wpb):
 def test_pipelined_helpers_bit_identical(cors, accumulation):
     """The launch shapes of one HO run (N = 128, S = 3: 16 segment threads per walker):
     2 walkers per CTA pipeline 32 helper threads per walker (a pair of lanes per 4 lags, the
-    correlator values from a path snapshot) behind the movers, in two helper sets that take
-    the measurements in turn (one set with more than 4 correlators); 1 walker per CTA leaves
-    the movers in half warps, so every thread of 4 groups sums one lag after the moves.
-    Paths, operators and accepts are bit-identical; so are the correlator sums of one helper
-    set, while two sets add their FP64 running sums at the end (equal up to the order of
-    the FP64 additions).  IEEE builds:
+    correlator values from a path snapshot) one measurement behind the movers; 1 walker per
+    CTA leaves the movers in half warps, so every thread of 4 groups sums one lag after the
+    moves.  Each sum is formed in the same order either way, so paths, operators, accepts
+    and correlator sums are bit-identical.  IEEE builds:
     with contraction allowed, the compiler may fuse x1 * x1 - 0.5 into one FMA at one call
     site and not at another, and the two shapes evaluate it at different call sites."""
     require_gpu()
     W, N = 256, 128
     kp = _kernel("fp32", True, N, 3, W, wpb=2, fast=False, cors=cors, accumulation=accumulation)
     kh = _kernel("fp32", True, N, 3, W, wpb=1, fast=False, cors=cors, accumulation=accumulation)
-    sets = 2 if len(cors) <= 4 else 1
-    assert (kp._info.walkers_per_block, kp._info.block_threads) == (2, 2 * 16 * (1 + 2 * sets))
+    assert (kp._info.walkers_per_block, kp._info.block_threads) == (2, 2 * 16 * 3)
     assert (kh._info.walkers_per_block, kh._info.block_threads) == (1, 16 * 4)
     p0 = (np.random.RandomState(6).randn(W, N) * 0.7).astype(np.float32)
     for k in (kp, kh):
@@ -100,10 +97,6 @@ def test_pipelined_helpers_bit_identical(cors, accumulation):
     assert np.array_equal(kp.getPaths(), kh.getPaths())
     assert np.array_equal(kp._raw_operators(), kh._raw_operators())
     assert np.array_equal(kp.getAccepts(), kh.getAccepts())
-    if sets == 1:
-        assert np.array_equal(kp._raw_correlator(), kh._raw_correlator())
-    else:
-        b = kh._raw_correlator()
-        np.testing.assert_allclose(kp._raw_correlator(), b, rtol=1e-13, atol=1e-13 * np.abs(b).max())
+    assert np.array_equal(kp._raw_correlator(), kh._raw_correlator())
     kp.close()
     kh.close()
