@@ -1189,11 +1189,19 @@ extern "C" int fs_run_host(fs_handle *h, const void *paths_in, void *paths_out, 
     CUDA_TRY(h, cudaStreamWaitEvent(h->s_out, h->ev0, 0), FS_ERR_CUDA);
     CUDA_TRY(h, cudaStreamWaitEvent(h->s_comp2, h->ev0, 0), FS_ERR_CUDA);
     // chunks alternate between two compute streams, so one chunk's last wave overlaps the
-    // next chunk's first (they touch disjoint walkers; shared histograms use atomics)
+    // next chunk's first (they touch disjoint walkers; shared histograms use atomics).  With
+    // three or more chunks the first and the last are a third of the others: only the first
+    // chunk's copy in and the last chunk's copy out are not hidden behind sweeps.
     cudaStream_t comp[2] = {h->stream, h->s_comp2};
+    const long long wsum = n_chunks >= 3 ? 3ll * (n_chunks - 2) + 2 : n_chunks;
+    auto cut = [&](int k) -> int {  // first CTA of chunk k (k = n_chunks: the grid)
+        long long wk = n_chunks >= 3 ? (k == 0 ? 0 : 1 + 3ll * (std::min(k, n_chunks - 1) - 1) + (k == n_chunks ? 1 : 0))
+                                     : k;
+        return (int)((long long)h->grid * wk / wsum);
+    };
     for (int k = 0; k < n_chunks; k++) {
-        const int cta0 = (int)((long long)h->grid * k / n_chunks);
-        const int cta1 = (int)((long long)h->grid * (k + 1) / n_chunks);
+        const int cta0 = cut(k);
+        const int cta1 = cut(k + 1);
         const size_t w0 = (size_t)cta0 * h->wpb;
         const size_t w1 = std::min((size_t)cta1 * h->wpb, (size_t)c.n_walkers);
         if (cta1 <= cta0 || w1 <= w0) continue;
