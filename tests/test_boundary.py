@@ -101,6 +101,16 @@ def test_config_errors(kw, msg):
     assert rc == -1 and msg in log
 
 
+def test_mlp_train_step_rejects_misaligned_buffers():
+    # checked before any device work: the pointers are never dereferenced
+    L = _lib()
+    rc = L.lib().fs_mlp_train_step(ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1002), ctypes.c_void_p(0x2000),
+                                   ctypes.c_void_p(0x3000), ctypes.c_void_p(0x4000), 128, 6,
+                                   ctypes.c_float(1.0 / 128), None, None)
+    assert rc == L.FS_ERR_CONFIG
+    assert b"16-byte aligned" in L.lib().fs_last_error(None)
+
+
 def test_python_validation_matches_reference_messages():
     from feynsimul_gb300.kernel import PIMCKernel
     from feynsimul_gb300.kernel_args import KernelArgs
