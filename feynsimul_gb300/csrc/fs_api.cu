@@ -646,14 +646,13 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
         // movers copy their slices to a double-buffered path snapshot, and the helpers alone
         // evaluate the correlator values on it and sum the lags, one measurement behind the
         // moves.
-        // The pipelined helpers give each pair of threads 4 consecutive lags (N/4 lag threads
-        // per walker, in pairs of one walker: an even number of segment threads) and sum
-        // FP32 partials over the doubled slice values.
+        // The pipelined helpers give each thread 4 consecutive lags (N/8 lag threads per
+        // walker) and sum FP32 partials over the doubled slice values.
         if (!h->cors.empty() && c.enable_parallelize_path && !c.global_path && !c.learned && h->tpw <= 32) {
             const int lag_threads = std::min(c.n_slices / 2, 64);
             const int wpw = 32 / h->tpw;
             const int wpb_min = c.walkers_per_block > 0 ? c.walkers_per_block : wpw;
-            const int groups = (c.n_slices / 4 + h->tpw - 1) / h->tpw;
+            const int groups = (c.n_slices / 8 + h->tpw - 1) / h->tpw;
             const bool fma_partials = (c.accum == FS_ACCUM_FP64 || c.accum == FS_ACCUM_KAHAN) &&
                                       !c.enable_double && c.partials == FS_PARTIALS_FP32;
             if (fma_partials && c.n_slices % 8 == 0 && c.n_slices >= 16 && h->tpw >= 2 && c.n_walkers % wpw == 0 &&

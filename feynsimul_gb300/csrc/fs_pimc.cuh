@@ -48,8 +48,8 @@
 #define FS_BLOCK (FS_MBLOCK * FS_MX)
 #define FS_CTPW (FS_TPW * (FS_MX - FS_PIPE))  // correlator threads per walker
 #if FS_PIPE
-#define FS_LPT 4                             // lags 2 lt .. 2 lt + 3 (even lt)
-#define FS_LAG(j) (2 * lt + (j))
+#define FS_LPT 4                             // lags 4 lt .. 4 lt + 3
+#define FS_LAG(j) (4 * lt + (j))
 #else
 #define FS_LPT ((FS_HALF_N + FS_CTPW - 1) / FS_CTPW)  // correlator lags owned per thread
 #define FS_LAG(j) (lt + (j) * FS_CTPW)
@@ -57,7 +57,7 @@
 #if FS_MX > 1 && (!FS_PARALLEL || FS_TPW > 32 || FS_GLOBAL || FS_NCOR == 0 || FS_NWALKERS % FS_WPB != 0)
 #error "correlator helpers need parallel-path walkers of at most 32 threads in shared memory, correlators, and full CTAs"
 #endif
-#if FS_PIPE && (FS_MX < 2 || FS_MBLOCK % 32 != 0 || FS_LEARNED || FS_SNSTRIDE < FS_DOF * (FS_N + (FS_N >> FS_S)) || FS_SNSTRIDE % 16 != 0 || FS_N % 8 != 0 || FS_CTPW < FS_N / 4 || FS_TPW % 2 != 0)
+#if FS_PIPE && (FS_MX < 2 || FS_MBLOCK % 32 != 0 || FS_LEARNED || FS_SNSTRIDE < FS_DOF * (FS_N + (FS_N >> FS_S)) || FS_SNSTRIDE % 16 != 0 || FS_N % 8 != 0 || FS_CTPW < FS_N / 8)
 #error "pipelined correlator helpers need helper groups, whole warps of movers and a path snapshot"
 #endif
 #define FS_COR_REGS (FS_ACCUM != 3 && FS_LPT * FS_NCOR <= 16)
@@ -625,10 +625,10 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
     const int wl = (tid_b - grp * FS_MBLOCK) / FS_TPW;
     const int t = tid_b % FS_TPW;
     const bool mover = FS_MX == 1 || grp == 0;
-    // this thread's lags FS_LAG(j): lt + j * FS_CTPW; with FS_PIPE the even helper lanes
-    // lt < N/4 own lags 2 lt + j
+    // this thread's lags FS_LAG(j): lt + j * FS_CTPW; with FS_PIPE the helper lanes lt < N/8
+    // own lags 4 lt + j
     const int lt = (grp - FS_PIPE) * FS_TPW + t;
-    const bool lagger = FS_PIPE ? !mover && lt < FS_N / 4 && (lt & 1) == 0 : true;
+    const bool lagger = FS_PIPE ? !mover && lt < FS_N / 8 : true;
     const int w0 = (blockIdx.x + a.block_offset) * FS_WPB;
     const int w = w0 + wl;
     const int n_here = min(FS_WPB, FS_NWALKERS - w0);
@@ -1051,53 +1051,45 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             }
         };
 #else
-        // pipelined helpers: a pair of lanes (lt = 2 p + h) sums lags 4 p .. 4 p + 3 of one
-        // measurement, lane h the chains of slices s1 = 2 h, 2 h + 1 (mod 4); the same four
-        // chains per lag in slice order and the same pairwise combination as the lag sums
-        // above, so the same bits: lane h adds its two chains, the even lane adds the odd
-        // lane's pair sum (a shuffle) and owns the FP64 sums.  8-byte loads: the slice pair
-        // s1 + 2h, s1 + 2h + 1 and the window s1 + 4p + 2h .. + 4, the window's upper half
-        // carried to the next step (3 loads per 8 products).  Reads stop at slice
-        // 3N/2 - 1 of the doubled values.  Every helper lane runs it (the shuffles).
+        // pipelined helpers: helper lane lt < N/8 sums lags 4 lt .. 4 lt + 3 of one
+        // measurement with the same four chains per lag (slices s1 mod 4, in slice order) and
+        // the same pairwise combination as the lag sums above, so the same bits; the slice
+        // values s1..s1+3 and the window s1 + 4 lt .. s1 + 4 lt + 7 come in 16-byte loads (2
+        // per 16 products), the window's upper half carried to the next step.  Reads stop at
+        // slice 4 lt + N + 3 < 3N/2 of the doubled values.
         auto fs_cor_lags4 = [&](const FT *Cm) {
-            const bool on = lt < FS_N / 4;
-            const int p = lt >> 1, h = lt & 1;
+            if (!(lt < FS_N / 8)) return;
 #pragma unroll
             for (int c = 0; c < FS_NCOR; c++) {
-                float sp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-                if (on) {
-                    const float2 *cv2 = reinterpret_cast<const float2 *>(Cm + c * FS_CSTRIDE);
-                    const float2 *wv2 = cv2 + 2 * p + h;
-                    float pa[4][2];
+                const float4 *cv4 = reinterpret_cast<const float4 *>(Cm + c * FS_CSTRIDE);
+                const float4 *wv4 = cv4 + lt;
+                float pa[4][4];
 #pragma unroll
-                    for (int j = 0; j < 4; j++) pa[j][0] = pa[j][1] = 0.0f;
-                    float2 w0 = wv2[0];
+                for (int j = 0; j < 4; j++)
+#pragma unroll
+                    for (int k = 0; k < 4; k++) pa[j][k] = 0.0f;
+                float4 w0 = wv4[0];
 #pragma unroll 32
-                    for (int q = 0; q < FS_N / 4; q++) {
-                        const float2 a2 = cv2[2 * q + h];
-                        const float2 w1 = wv2[2 * q + 1], w2 = wv2[2 * q + 2];
-                        const float wv[5] = {w0.x, w0.y, w1.x, w1.y, w2.x};
+                for (int q = 0; q < FS_N / 4; q++) {
+                    const float4 a4 = cv4[q];
+                    const float4 w1 = wv4[q + 1];
+                    const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+                    const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
-                        for (int j = 0; j < 4; j++) {
-                            pa[j][0] = __fmaf_rn(a2.x, wv[j], pa[j][0]);
-                            pa[j][1] = __fmaf_rn(a2.y, wv[j + 1], pa[j][1]);
-                        }
-                        w0 = w2;
-                    }
+                    for (int j = 0; j < 4; j++)
 #pragma unroll
-                    for (int j = 0; j < 4; j++) sp[j] = __fadd_rn(pa[j][0], pa[j][1]);
+                        for (int k = 0; k < 4; k++) pa[j][k] = __fmaf_rn(av[k], wv[k + j], pa[j][k]);
+                    w0 = w1;
                 }
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    const float o = __shfl_down_sync(0xffffffffu, sp[j], 1);
-                    if (lagger) {
-                        const double m = fs_f2d(__fadd_rn(sp[j], o));
+                    const double m =
+                        fs_f2d(__fadd_rn(__fadd_rn(pa[j][0], pa[j][1]), __fadd_rn(pa[j][2], pa[j][3])));
 #if FS_COR_REGS
-                        cacc[c][j] = __dadd_rn(cacc[c][j], m);
+                    cacc[c][j] = __dadd_rn(cacc[c][j], m);
 #else
-                        g_cor[c * FS_HALF_N + FS_LAG(j)] = __dadd_rn(g_cor[c * FS_HALF_N + FS_LAG(j)], m);
+                    g_cor[c * FS_HALF_N + FS_LAG(j)] = __dadd_rn(g_cor[c * FS_HALF_N + FS_LAG(j)], m);
 #endif
-                    }
                 }
             }
         };

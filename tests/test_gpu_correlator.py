@@ -40,8 +40,8 @@ def _kernel(partials, parallel, N, S, W=256, wpb=0, fast=True, cors=COR2, accumu
 
 
 @pytest.mark.parametrize("parallel,N,S,wpb", [
-    (True, 128, 3, 0),   # 16 segment threads + 32 pipelined helpers, a lane pair per 4 lags
-    (True, 64, 2, 0),    # 16 segment threads + 16 pipelined helpers, a lane pair per 4 lags
+    (True, 128, 3, 0),   # 16 segment threads + 16 pipelined helpers, 4 lags each
+    (True, 64, 2, 0),    # 16 segment threads + 16 pipelined helpers, 8 of them 4 lags each
     (True, 128, 3, 1),   # movers in half warps: 16 + 48 helpers after the moves, one lag each
     (True, 256, 2, 0),   # 64 segment threads, two lags each, no helpers
     (False, 64, 2, 0),   # one thread per walker: all 32 lags in one loop, sums in device memory
@@ -75,10 +75,9 @@ def test_fp32_partials_within_bound_of_float_float(parallel, N, S, wpb):
                          ids=["two_correlators", "five_correlators", "kahan"])
 def test_pipelined_helpers_bit_identical(cors, accumulation):
     """The launch shapes of one HO run (N = 128, S = 3: 16 segment threads per walker):
-    2 walkers per CTA pipeline 32 helper threads per walker (a pair of lanes per 4 lags, the
-    correlator values from a path snapshot) one measurement behind the movers; 1 walker per
-    CTA leaves the movers in half warps, so every thread of 4 groups sums one lag after the
-    moves.  Each sum is formed in the same order either way, so paths, operators, accepts
+    2 walkers per CTA pipeline 16 helper threads per walker (4 lags each, the correlator
+    values from a path snapshot) one measurement behind the movers; 1 walker per CTA leaves
+    the movers in half warps, so every thread of 4 groups sums one lag after the moves.  Each sum is formed in the same order either way, so paths, operators, accepts
     and correlator sums are bit-identical.  IEEE builds:
     with contraction allowed, the compiler may fuse x1 * x1 - 0.5 into one FMA at one call
     site and not at another, and the two shapes evaluate it at different call sites."""
@@ -86,7 +85,7 @@ def test_pipelined_helpers_bit_identical(cors, accumulation):
     W, N = 256, 128
     kp = _kernel("fp32", True, N, 3, W, wpb=2, fast=False, cors=cors, accumulation=accumulation)
     kh = _kernel("fp32", True, N, 3, W, wpb=1, fast=False, cors=cors, accumulation=accumulation)
-    assert (kp._info.walkers_per_block, kp._info.block_threads) == (2, 2 * 16 * 3)
+    assert (kp._info.walkers_per_block, kp._info.block_threads) == (2, 2 * 16 * 2)
     assert (kh._info.walkers_per_block, kh._info.block_threads) == (1, 16 * 4)
     p0 = (np.random.RandomState(6).randn(W, N) * 0.7).astype(np.float32)
     for k in (kp, kh):
