@@ -169,17 +169,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) fs_mlp_infer_tc_kernel(const ui
 // the 128-row tiles.
 int fsi_mlp_infer_tc(const void *frag, const float *bias, const float *x, float *y, int n_rows, cudaStream_t s)
 {
-    static int smem_set = -1;
-    static int sms = 0;
-    if (smem_set < 0) {
+    // per call: the attribute belongs to the current device (a process may use several)
+    {
         cudaError_t e = cudaFuncSetAttribute(fs_mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)sizeof(TcSmem));
         if (e != cudaSuccess) return fsi_thread_error(FS_ERR_CUDA, cudaGetErrorString(e));
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        smem_set = 1;
     }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
     const int n_tiles = (n_rows + TC_M - 1) / TC_M;
     const int grid = n_tiles < 2 * sms ? n_tiles : 2 * sms;
     fs_mlp_infer_tc_kernel<<<grid, TC_THREADS, sizeof(TcSmem), s>>>((const uint2 *)frag, bias, x, y, n_rows);

@@ -465,16 +465,14 @@ extern "C" int fs_mlp_train_step(const float *params, const uint16_t *wq, float 
         return fsi_thread_error(FS_ERR_CONFIG, "fs_mlp_train_step: need 1 <= dof <= 8 and n_rows >= 1");
     if (((uintptr_t)wq | (uintptr_t)x | (uintptr_t)grad) & 15u)
         return fsi_thread_error(FS_ERR_CONFIG, "fs_mlp_train_step: wq, x and grad must be 16-byte aligned");
-    static int sms = 0;
-    if (!sms) {
-        cudaError_t e = cudaFuncSetAttribute(fs_mlp_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)TT_SMEM_BYTES);
-        if (e != cudaSuccess) return fsi_thread_error(FS_ERR_CUDA, cudaGetErrorString(e));
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms < 1) sms = 1;
-    }
+    // per call: the attribute belongs to the current device (a process may use several)
+    cudaError_t e = cudaFuncSetAttribute(fs_mlp_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)TT_SMEM_BYTES);
+    if (e != cudaSuccess) return fsi_thread_error(FS_ERR_CUDA, cudaGetErrorString(e));
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms < 1) sms = 1;
     const int n_tiles = (n_rows + 127) / 128;
     fs_mlp_train_tc_kernel<<<n_tiles < sms ? n_tiles : sms, TT_THREADS, TT_SMEM_BYTES, (cudaStream_t)stream>>>(
         params, (const fs_bf16 *)wq, grad, x, z, n_rows, dof, inv_batch, loss);
