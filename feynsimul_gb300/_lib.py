@@ -36,7 +36,8 @@ EXPORTS = (
     "fs_set_bins", "fs_set_histogram", "fs_mlp_sizes", "fs_mlp_train_step", "fs_mlp_adam",
     "fs_mlp_pack", "fs_mlp_infer", "fs_set_learned_proposal", "fs_batch_create", "fs_batch_destroy",
     "fs_batch_run", "fs_batch_sync", "fs_batch_get_run_time", "fs_batch_set_paths", "fs_batch_get_paths",
-    "fs_batch_set_seeds", "fs_batch_get_op_sums", "fs_batch_get_accepts", "fs_batch_query",
+    "fs_batch_set_seeds", "fs_batch_init_ranlux", "fs_batch_get_ranlux_tables", "fs_batch_get_op_sums",
+    "fs_batch_get_accepts", "fs_batch_query",
     "fs_reduce_correlator", "fs_set_paths_tiled", "fs_get_step_counter", "fs_set_step_counter",
     "fs_run_host", "fs_pin_host", "fs_unpin_host", "fs_get_walker_operators", "fs_get_last_chunks",
 )
@@ -142,7 +143,9 @@ _PROTOS = {
     "fs_mlp_pack": ([_P, _P, _P, _P, _P], ctypes.c_int),
     "fs_mlp_infer": ([_P, _P, _P, _P, _I, _P], ctypes.c_int),
     "fs_set_learned_proposal": ([_P, _P, _S, _P, _S, ctypes.c_double], ctypes.c_int),
-    "fs_batch_create": ([_I, _P, _STRS, _STRS, _STRS, _I, _I, _P, _I, _I, _I, ctypes.POINTER(_P)], ctypes.c_int),
+    "fs_batch_create": ([_I, _P, _STRS, _STRS, _STRS, _I, _I, _P, _I, _I, _I, _I, ctypes.POINTER(_P)], ctypes.c_int),
+    "fs_batch_init_ranlux": ([_P, _I, _P, _S, _P, _S], ctypes.c_int),
+    "fs_batch_get_ranlux_tables": ([_P, _I, _P, _S, _P, _S], ctypes.c_int),
     "fs_batch_destroy": ([_P], ctypes.c_int),
     "fs_batch_run": ([_P, _I, _I], ctypes.c_int),
     "fs_batch_sync": ([_P], ctypes.c_int),

@@ -64,7 +64,12 @@ class BatchSampler:
     """One persistent launch over all systems of a workload (list of dicts with n, N, T,
     walkers)."""
 
-    def __init__(self, workload, op_runs=1, msteps=4, block_threads=256, tpw_target=16, seed=0, noise=0.0):
+    def __init__(self, workload, op_runs=1, msteps=4, block_threads=256, tpw_target=16, seed=0, noise=0.0,
+                 ranlux=None):
+        """ranlux: None for xorshift streams, or a luxuaryFactor (the kernel uses +1, as
+        KernelArgs.luxuaryFactor) for RANLUX tables, seeded per system like the sweep's fixed
+        mode: thread row r from (s << 32) + r, walker row w from ((s ^ 2^31) << 32) + w, s a
+        31-bit seed drawn per system."""
         from .physical_systems.lm2m2 import Lm2m2Cluster
         self.workload = workload
         ns = sorted({w["n"] for w in workload})
@@ -84,8 +89,9 @@ class BatchSampler:
         ucs, _ = strings([clusters[n].userCode for n in ns])
         ops, _ = strings([clusters[n].energyOp for n in ns])
         h = ctypes.c_void_p()
+        self.ranlux = ranlux
         check(lib().fs_batch_create(len(ns), dofs, pots, ucs, ops, 1, len(self.systems), arr, op_runs, msteps,
-                                    block_threads, ctypes.byref(h)))
+                                    block_threads, -1 if ranlux is None else int(ranlux), ctypes.byref(h)))
         self._h = h
         L = lib()
         nu, sm, rg, ni, gr = (ctypes.c_int64() for _ in range(5))
@@ -104,6 +110,21 @@ class BatchSampler:
             ts = rng.randint(0, 2 ** 31 - 1, size=(w["walkers"] * tpw, 4)).astype(np.uint32)
             ws = rng.randint(0, 2 ** 31 - 1, size=(w["walkers"], 4)).astype(np.uint32)
             check(L.fs_batch_set_seeds(h, i, ts.ctypes.data, ts.shape[0], ws.ctypes.data, ws.shape[0]))
+            if ranlux is not None:
+                base = int(rng.randint(0, 2 ** 31 - 1))
+                xt = (np.uint64(base) << np.uint64(32)) + np.arange(ts.shape[0], dtype=np.uint64)
+                xw = (np.uint64(base ^ 0x80000000) << np.uint64(32)) + np.arange(ws.shape[0], dtype=np.uint64)
+                check(L.fs_batch_init_ranlux(h, i, xt.ctypes.data, xt.size, xw.ctypes.data, xw.size))
+
+    def ranlux_tables(self, i):
+        """System i's RANLUX tables (thread rows [threads][28], walker rows [walkers][28],
+        uint32, the reference's layout)."""
+        s = self.systems[i]
+        nt = s.n_walkers * (s.n_slices >> s.bisection_level)
+        t = np.empty((nt, 28), np.uint32)
+        g = np.empty((s.n_walkers, 28), np.uint32)
+        check(lib().fs_batch_get_ranlux_tables(self._h, i, t.ctypes.data, nt, g.ctypes.data, s.n_walkers))
+        return t, g
 
     def set_state(self, i, paths, thread_seeds, walker_seeds):
         """Replace system i's paths [walkers, DOF*N] and xorshift rows ([walkers*tpw][4] per

@@ -390,6 +390,7 @@ static int compile_module(fs_handle *h, const std::string &src, bool fast, std::
 __attribute__((visibility("hidden"))) std::string fsi_float_literals(const std::string &s) { return float_literals(s); }
 __attribute__((visibility("hidden"))) std::string fsi_prelude(bool dbl) { return gen_prelude(dbl); }
 __attribute__((visibility("hidden"))) const char *fsi_rng_src() { return kRngSrc; }
+__attribute__((visibility("hidden"))) int fsi_nskip_for(int lux) { return nskip_for(lux); }
 __attribute__((visibility("hidden"))) const char *fsi_batch_src();
 __attribute__((visibility("hidden"))) int fsi_compile(const std::string &src, bool fast, std::string *cubin,
                                                       std::string *log)

@@ -8,7 +8,7 @@
 // A work item is a tile of walkers of one system.  CTAs pull items from a global counter
 // (largest first, so the ragged tail is short) and run all the launch's sweeps on the
 // tile: the same Metropolis-bisection move as fs_pimc.cuh (kernel.c:258-399, with the
-// fixed-mode xorshift streams), but N, S, epsilon, the bisection widths and the walker
+// fixed-mode xorshift or RANLUX streams), but N, S, epsilon, the bisection widths and the walker
 // counts are runtime values of the system, the path tile lives in shared memory while the
 // saved old segments go to the CTA's slice of a global scratch buffer (a 27-DOF,
 // 1024-slice walker's path alone takes 117 KB), and a walker wider than a warp
@@ -16,12 +16,35 @@
 #pragma once
 
 #define FS_BATCH_MAX_S 10
+#ifndef FSB_RANLUX
+#define FSB_RANLUX 0
+#endif
+
+// the batch's random streams: per segment thread (node draws, acceptance) and per walker
+// (the segment offset; every thread of the walker advances its own identical copy), as the
+// sweep's fixed mode: xorshift rows or RANLUX tables (luxury FS_NSKIP for the whole batch)
+#if FSB_RANLUX
+typedef FsRanluxStream<FS_NSKIP> FsbStream;
+__device__ __forceinline__ float fsb_uniform(FsbStream &g) { return g.next(); }
+__device__ __forceinline__ fs_u32 fsb_offset(FsbStream &g, fs_u32 range)
+{
+    return ((fs_u32)__fmul_rn(g.next(), (float)range)) & (range - 1u);  // kernel.c:715-718, fixed mode
+}
+#define FSB_DRAW_UNROLL _Pragma("unroll 1")  // one inlined generator per move loop
+#else
+typedef FsXorshift FsbStream;
+__device__ __forceinline__ float fsb_uniform(FsbStream &g) { return fs_xs_float(g); }
+__device__ __forceinline__ fs_u32 fsb_offset(FsbStream &g, fs_u32 range) { return fs_xs_next(g) & (range - 1u); }
+#define FSB_DRAW_UNROLL _Pragma("unroll")
+#endif
 
 struct FsBatchSys {
     float *paths;            // [walkers][DOF][N]
     float *old_scratch;      // per CTA slot: saved segments [(seg-1)*DOF][tile threads]
     fs_u32 *seeds;           // [threads][4]  (thread = walker * tpw + t)
     fs_u32 *wseeds;          // [walkers][4]
+    fs_u32 *rtab;            // RANLUX: [threads][28] (the reference's table layout)
+    fs_u32 *gtab;            // RANLUX: [walkers][28]
     fs_u32 *accepts;         // [threads]
     double *op_sums;         // [walkers][nops], accumulated over launches
     int n_walkers, N, S, tpw, wpb, nops, type, n_tiles;
@@ -87,12 +110,19 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
         const int w = w0 + wl;
         float *P = GLOBAL ? sd.paths + (size_t)w * DOF * N : smem + wl * wstride;
         const int th = w * tpw + t;
-        FsXorshift g, ws;
+        FsbStream g, ws;
         {
+#if FSB_RANLUX
+            fs_rl_load(g.st, sd.rtab + (size_t)th * 28);
+            g.count = 0u;
+            fs_rl_load(ws.st, sd.gtab + (size_t)w * 28);
+            ws.count = 0u;
+#else
             const uint4 s4 = *(const uint4 *)(sd.seeds + (size_t)th * 4);
             g.x = s4.x; g.y = s4.y; g.z = s4.z; g.w = s4.w;
             const uint4 g4 = *(const uint4 *)(sd.wseeds + (size_t)w * 4);
             ws.x = g4.x; ws.y = g4.y; ws.z = g4.z; ws.w = g4.w;
+#endif
         }
         fs_u32 n_acc = 0u;
         double opd[Sys::NOPS > 0 ? Sys::NOPS : 1];
@@ -103,7 +133,7 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
         for (int run = 0; run < sd.op_runs; run++) {
 #pragma unroll 1
             for (int step = 0; step < sd.msteps; step++) {
-                const fs_u32 off = fs_xs_next(ws) & (fs_u32)(seg - 1);
+                const fs_u32 off = fsb_offset(ws, (fs_u32)seg);
                 const int start = (int)((off + (fs_u32)(seg * t)) & (fs_u32)(N - 1));
                 // ---- bisection move (kernel.c:258-399) ----
                 float aOld = 0.f, aNew = 0.f;
@@ -127,9 +157,10 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
                         const int m = ((1 + 2 * i) * half + start) & (N - 1);
                         const int l = (i * 2 * half + start) & (N - 1);
                         const int r = ((i + 1) * 2 * half + start) & (N - 1);
-#pragma unroll
+                        FSB_DRAW_UNROLL
                         for (int d = 0; d < DOF; d++) {
-                            const float u = fs_xs_float(g), v = fs_xs_float(g);
+                            const float u = fsb_uniform(g);
+                            const float v = fsb_uniform(g);
                             // evaluated for every degree of freedom and replaced by 0 where
                             // v == 0 (kernel.c:349-353): no branch, so the compiler
                             // interleaves the degrees of freedom
@@ -147,7 +178,7 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
                     for (int d = 0; d < DOF; d++) x[d] = FSB_AT(P, d, p);
                     aNew = __fadd_rn(aNew, __fmul_rn(eps, Sys::pot(x)));
                 }
-                if (__expf(__fsub_rn(aOld, aNew)) < fs_xs_float(g)) {
+                if (__expf(__fsub_rn(aOld, aNew)) < fsb_uniform(g)) {
 #pragma unroll 1
                     for (int i = 1; i < seg; i++) {
                         const int p = (start + i) & (N - 1);
@@ -181,8 +212,13 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
             fs_walker_sync(tpw, wl);
         }
         sd.accepts[th] = n_acc;
+#if FSB_RANLUX
+        fs_rl_store(g.st, sd.rtab + (size_t)th * 28);
+        if (t == 0) fs_rl_store(ws.st, sd.gtab + (size_t)w * 28);
+#else
         *(uint4 *)(sd.seeds + (size_t)th * 4) = make_uint4(g.x, g.y, g.z, g.w);
         if (t == 0) *(uint4 *)(sd.wseeds + (size_t)w * 4) = make_uint4(ws.x, ws.y, ws.z, ws.w);
+#endif
 #pragma unroll
         for (int k = 0; k < Sys::NOPS; k++) atomicAdd(s_op + wl * Sys::NOPS + k, opd[k]);
     }

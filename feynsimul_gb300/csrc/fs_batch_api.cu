@@ -21,6 +21,7 @@ std::string fsi_float_literals(const std::string &s);
 std::string fsi_prelude(bool dbl);
 const char *fsi_rng_src();
 const char *fsi_batch_src();
+int fsi_nskip_for(int lux);
 int fsi_compile(const std::string &src, bool fast, std::string *cubin, std::string *log);
 
 #define FS_BATCH_MAX_S 10
@@ -28,7 +29,7 @@ int fsi_compile(const std::string &src, bool fast, std::string *cubin, std::stri
 struct FsBatchSysHost {  // mirrors FsBatchSys in fs_batch.cuh
     float *paths;
     float *old_scratch;
-    uint32_t *seeds, *wseeds, *accepts;
+    uint32_t *seeds, *wseeds, *rtab, *gtab, *accepts;
     double *op_sums;
     int n_walkers, N, S, tpw, wpb, nops, type, n_tiles;
     int op_runs, msteps;
@@ -44,6 +45,7 @@ struct fs_batch {
     std::vector<int> type_dof;
     std::vector<FsBatchSysHost> desc;
     int n_ops = 0, block = 256, grid = 0;
+    int lux = -1;  // RANLUX luxuaryFactor as the user gives it (the kernel uses +1); -1: xorshift
     size_t smem = 0, old_slot = 0;
     long long n_items = 0, node_updates = 0;
     int regs = 0;
@@ -108,10 +110,25 @@ static int balloc(fs_batch *b, void **p, size_t bytes)
     return FS_OK;
 }
 
+// RANLUX rows of a device table seeded by ranluxcl_init from xs (host), in slices of the
+// no-alloc seeding's row limit, in the batch's stream
+static int seed_rows(fs_batch *b, uint32_t *table, const uint64_t *xs, size_t n_rows)
+{
+    const size_t slice = 1u << 18;
+    for (size_t r = 0; r < n_rows; r += slice) {
+        const size_t n = std::min(slice, n_rows - r);
+        int rc = fs_ranlux_init_noalloc(table + r * 28, xs + r, n, b->stream);
+        if (rc) return rc;
+        cudaError_t e = cudaStreamSynchronize(b->stream);  // the seeding's scratch is reused
+        if (e != cudaSuccess) return bfail(FS_ERR_CUDA, "ranlux seeding: %s", cudaGetErrorString(e));
+    }
+    return FS_OK;
+}
+
 extern "C" int fs_batch_create(int32_t n_types, const int32_t *type_dof, const char *const *potentials,
                                const char *const *user_codes, const char *const *operators, int32_t n_ops,
                                int32_t n_systems, const fs_batch_system *systems, int32_t op_runs,
-                               int32_t msteps, int32_t block_threads, fs_batch **out)
+                               int32_t msteps, int32_t block_threads, int32_t ranlux_luxury, fs_batch **out)
 {
     if (!out || n_types < 1 || n_systems < 1 || !type_dof || !potentials || !systems)
         return bfail(FS_ERR_CONFIG, "fs_batch_create: bad arguments");
@@ -119,9 +136,17 @@ extern "C" int fs_batch_create(int32_t n_types, const int32_t *type_dof, const c
         return bfail(FS_ERR_CONFIG, "fs_batch_create: 0..4 operators, op_runs >= 1, msteps >= 0");
     if (block_threads < 32 || block_threads > 1024 || block_threads % 32)
         return bfail(FS_ERR_CONFIG, "fs_batch_create: block_threads must be a multiple of 32 in [32, 1024]");
+    if (ranlux_luxury != -1) {
+        // the single-system rule (fs_create): luxury 0-3, or >= 23 with p - 24 a multiple of 4
+        const int lux = ranlux_luxury + 1, ns = fsi_nskip_for(lux);
+        if (ranlux_luxury < 0 || (lux > 4 && lux < 24) || ns % 4 != 0 || (ns != 0 && ns < 24))
+            return bfail(FS_ERR_CONFIG, "fs_batch_create: ranlux_luxury must be -1 (xorshift), 0-3, or >= 23 "
+                                        "with p - 24 a multiple of 4");
+    }
     *out = nullptr;
     fs_batch *b = new fs_batch();
     b->block = block_threads;
+    b->lux = ranlux_luxury;
     b->n_ops = n_ops;
     b->type_dof.assign(type_dof, type_dof + n_types);
     b->sys.assign(systems, systems + n_systems);
@@ -172,7 +197,8 @@ extern "C" int fs_batch_create(int32_t n_types, const int32_t *type_dof, const c
 
     // ---- source: prelude, RNG, one namespace per type, batch kernel, dispatcher ----
     std::ostringstream o;
-    o << fsi_prelude(false) << "#define FS_NSKIP 0\n" << fsi_rng_src() << "\n";
+    o << fsi_prelude(false) << "#define FS_NSKIP " << (b->lux >= 0 ? fsi_nskip_for(b->lux + 1) : 0)
+      << "\n#define FSB_RANLUX " << (b->lux >= 0 ? 1 : 0) << "\n" << fsi_rng_src() << "\n";
     for (int k = 0; k < n_types; k++) {
         const int dof = b->type_dof[k];
         // scalar-argument bodies; called rather than inlined for more than 8 DOF (see the
@@ -298,6 +324,17 @@ extern "C" int fs_batch_create(int32_t n_types, const int32_t *type_dof, const c
         CT(balloc(b, &p, W * dof * s.n_slices * 4)); d.paths = (float *)p;
         CT(balloc(b, &p, T * 16)); d.seeds = (uint32_t *)p;
         CT(balloc(b, &p, W * 16)); d.wseeds = (uint32_t *)p;
+        if (b->lux >= 0) {
+            // RANLUX tables, seeded with distinct default values per system and row (callers
+            // re-seed with fs_batch_init_ranlux)
+            CT(balloc(b, &p, T * 28 * 4)); d.rtab = (uint32_t *)p;
+            CT(balloc(b, &p, W * 28 * 4)); d.gtab = (uint32_t *)p;
+            std::vector<uint64_t> xs(std::max(T, W));
+            for (size_t r = 0; r < T; r++) xs[r] = ((uint64_t)(0x5EED0000u + (unsigned)i) << 32) + r;
+            CT(seed_rows(b, d.rtab, xs.data(), T));
+            for (size_t r = 0; r < W; r++) xs[r] = ((uint64_t)(0x7EED0000u + (unsigned)i) << 32) + r;
+            CT(seed_rows(b, d.gtab, xs.data(), W));
+        }
         CT(balloc(b, &p, T * 4)); d.accepts = (uint32_t *)p;
         CT(balloc(b, &p, W * std::max(n_ops, 1) * 8)); d.op_sums = (double *)p;
         d.old_scratch = (float *)b->d_old;
@@ -423,6 +460,30 @@ extern "C" int fs_batch_set_seeds(fs_batch *b, int32_t i, const uint32_t *thread
     int rc = sys_copy(b, i, d.seeds, (void *)thread_rows, n_threads * 16, (size_t)d.n_walkers * d.tpw * 16, true);
     if (!rc) rc = sys_copy(b, i, d.wseeds, (void *)walker_rows, n_walkers * 16, (size_t)d.n_walkers * 16, true);
     return rc;
+}
+
+extern "C" int fs_batch_init_ranlux(fs_batch *b, int32_t i, const uint64_t *xs_threads, size_t n_threads,
+                                    const uint64_t *xs_walkers, size_t n_walkers)
+{
+    if (!b || i < 0 || i >= (int)b->sys.size()) return bfail(FS_ERR_CONFIG, "bad system index");
+    if (b->lux < 0) return bfail(FS_ERR_STATE, "the batch was created with xorshift streams");
+    const FsBatchSysHost &d = b->desc[i];
+    if (!xs_threads || !xs_walkers || n_threads != (size_t)d.n_walkers * d.tpw || n_walkers != (size_t)d.n_walkers)
+        return bfail(FS_ERR_IO, "system %d: %d thread seeds and %d walker seeds expected", i, d.n_walkers * d.tpw,
+                     d.n_walkers);
+    BT(cudaSetDevice(b->device));
+    int rc = seed_rows(b, d.rtab, xs_threads, n_threads);
+    return rc ? rc : seed_rows(b, d.gtab, xs_walkers, n_walkers);
+}
+
+extern "C" int fs_batch_get_ranlux_tables(fs_batch *b, int32_t i, uint32_t *thread_rows, size_t n_threads,
+                                          uint32_t *walker_rows, size_t n_walkers)
+{
+    if (!b || i < 0 || i >= (int)b->sys.size()) return bfail(FS_ERR_CONFIG, "bad system index");
+    if (b->lux < 0) return bfail(FS_ERR_STATE, "the batch was created with xorshift streams");
+    const FsBatchSysHost &d = b->desc[i];
+    int rc = sys_copy(b, i, d.rtab, thread_rows, n_threads * 28 * 4, (size_t)d.n_walkers * d.tpw * 28 * 4, false);
+    return rc ? rc : sys_copy(b, i, d.gtab, walker_rows, n_walkers * 28 * 4, (size_t)d.n_walkers * 28 * 4, false);
 }
 
 extern "C" int fs_batch_get_op_sums(fs_batch *b, int32_t i, double *out, size_t n)

@@ -336,10 +336,14 @@ typedef struct fs_batch_system {
     double beta;
     int32_t walkers_per_tile;  /* 0 = as many as fit the block (output: the value used) */
 } fs_batch_system;
+/* ranlux_luxury: -1 = xorshift streams (rows set by fs_batch_set_seeds); otherwise RANLUX
+ * tables for every system with luxuaryFactor ranlux_luxury (the kernel uses +1, as
+ * fs_config.luxury_factor), seeded with distinct default values per system and row and
+ * re-seeded by fs_batch_init_ranlux. */
 int fs_batch_create(int32_t n_types, const int32_t *type_dof, const char *const *potentials,
                     const char *const *user_codes, const char *const *operators, int32_t n_ops,
                     int32_t n_systems, const fs_batch_system *systems, int32_t op_runs,
-                    int32_t msteps, int32_t block_threads, fs_batch **out);
+                    int32_t msteps, int32_t block_threads, int32_t ranlux_luxury, fs_batch **out);
 int fs_batch_destroy(fs_batch *b);
 /* n_launches persistent launches; use_graph = 1 replays a captured CUDA graph (counter
  * reset + launch) instead of launching directly.  Asynchronous. */
@@ -350,6 +354,14 @@ int fs_batch_set_paths(fs_batch *b, int32_t system, const float *host, size_t n)
 int fs_batch_get_paths(fs_batch *b, int32_t system, float *host, size_t n);
 int fs_batch_set_seeds(fs_batch *b, int32_t system, const uint32_t *thread_rows, size_t n_threads,
                        const uint32_t *walker_rows, size_t n_walkers);
+/* RANLUX batches: system's tables seeded by ranluxcl_init, row r of the thread table from
+ * xs_threads[r] (thread = walker * threads per walker + t) and row w of the walker table
+ * (segment offsets) from xs_walkers[w]; and both tables read back (28 words per row, the
+ * reference's layout). */
+int fs_batch_init_ranlux(fs_batch *b, int32_t system, const uint64_t *xs_threads, size_t n_threads,
+                         const uint64_t *xs_walkers, size_t n_walkers);
+int fs_batch_get_ranlux_tables(fs_batch *b, int32_t system, uint32_t *thread_rows, size_t n_threads,
+                               uint32_t *walker_rows, size_t n_walkers);
 int fs_batch_get_op_sums(fs_batch *b, int32_t system, double *out, size_t n);
 int fs_batch_get_accepts(fs_batch *b, int32_t system, uint32_t *out, size_t n);
 int fs_batch_query(const fs_batch *b, int64_t *node_updates_per_launch, int64_t *smem_bytes,

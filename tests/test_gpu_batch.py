@@ -114,3 +114,54 @@ def test_batch_systems_match_oracle():
         e_o = o.op_means.reshape(w["walkers"], tpw).mean(axis=1)
         np.testing.assert_allclose(e_b[keep], e_o[keep], rtol=2e-3, atol=2e-3)
     b.close()
+
+
+def test_batch_systems_match_oracle_ranlux():
+    """The same per-system check with RANLUX streams (luxury 2, the kernel's 3: p = 224):
+    every system's tables after the launch equal the oracle's bit for bit (a move draws the
+    same count of numbers whatever its decision), and the accepts, paths and energies agree
+    as in the xorshift case."""
+    require_gpu()
+    engine()
+    from feynsimul_gb300.batch import BatchSampler
+    from oracle.oracle import OracleConfig, OracleSampler
+    workload = [{"n": 3, "N": 64, "T": 1.0, "walkers": 64}, {"n": 4, "N": 128, "T": 0.7, "walkers": 32},
+                {"n": 5, "N": 64, "T": 1.5, "walkers": 32}, {"n": 6, "N": 32, "T": 0.6, "walkers": 32}]
+    op_runs, msteps = 2, 3
+    b = BatchSampler(workload, op_runs=op_runs, msteps=msteps, block_threads=256, tpw_target=16, ranlux=2)
+    rng = np.random.RandomState(9)
+    oracles = []
+    for i, w in enumerate(workload):
+        c = b.clusters[w["n"]]
+        S = b.systems[i].bisection_level
+        tpw = w["N"] >> S
+        paths = c.initial_paths(w["walkers"], w["N"], rng).astype(np.float32)
+        ts = np.zeros((w["walkers"] * tpw, 4), np.uint32)
+        ws = np.zeros((w["walkers"], 4), np.uint32)
+        b.set_state(i, paths, ts, ws)  # the paths; the xorshift rows are unused here
+        t, g = b.ranlux_tables(i)
+        assert len({row.tobytes() for row in t}) == t.shape[0]  # distinct per thread
+        o = OracleSampler(OracleConfig(
+            DOF=c.DOF, potential=c.potential, userCode=c.userCode, nbrOfWalkers=w["walkers"], N=w["N"],
+            beta=float(1.0 / w["T"]), S=S, operatorRuns=op_runs, metroStepsPerOperatorRun=msteps,
+            enableRanlux=True, luxuaryFactor=2, operators=(c.energyOp,), compat=False, accum=1))
+        o.paths[...] = paths
+        o.ranlux_tab[...] = t
+        o.group_tab[...] = g
+        oracles.append(o)
+    b.run(1, graph=False)
+    for i, (w, o) in enumerate(zip(workload, oracles)):
+        o.run()
+        t, g = b.ranlux_tables(i)
+        assert np.array_equal(t, o.ranlux_tab), i
+        assert np.array_equal(g, o.group_tab), i
+        tpw = w["N"] >> b.systems[i].bisection_level
+        diff = b.accepts(i) != o.accepts
+        assert diff.mean() <= 0.05, (i, diff.mean())
+        keep = ~diff.reshape(w["walkers"], tpw).any(axis=1)
+        assert keep.mean() >= 0.5, (i, keep.mean())
+        np.testing.assert_allclose(b.paths(i)[keep], o.paths[keep], rtol=2e-3, atol=2e-4)
+        e_b = b.energy_sums(i) / (op_runs * w["N"])
+        e_o = o.op_means.reshape(w["walkers"], tpw).mean(axis=1)
+        np.testing.assert_allclose(e_b[keep], e_o[keep], rtol=2e-3, atol=2e-3)
+    b.close()
