@@ -1069,7 +1069,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #pragma unroll
                     for (int k = 0; k < 4; k++) pa[j][k] = 0.0f;
                 float4 w0 = wv4[0];
-#pragma unroll 8
+#pragma unroll 16
                 for (int q = 0; q < FS_N / 4; q++) {
                     const float4 a4 = cv4[q];
                     const float4 w1 = wv4[q + 1];
