@@ -76,6 +76,19 @@ def test_nvrtc_compiles_five_correlators():
     assert rc == 0, log
 
 
+@pytest.mark.parametrize("N,S,W,ncor,accum", [
+    (16, 1, 32, 1, 1), (16, 2, 8, 2, 1), (32, 3, 64, 1, 2), (64, 1, 64, 1, 1), (64, 2, 33, 1, 1),
+    (64, 3, 128, 3, 1), (128, 2, 64, 1, 1), (128, 3, 1024, 2, 0), (128, 4, 96, 1, 3), (256, 2, 32, 1, 1),
+    (256, 3, 64, 5, 1), (512, 4, 32, 1, 1), (1024, 5, 16, 1, 1), (64, 6, 64, 1, 1), (32, 5, 32, 1, 1),
+])
+def test_correlator_launch_shapes_compile(N, S, W, ncor, accum):
+    # the host's choice of correlator helpers (after the moves, pipelined, or none) and lag
+    # layout for a spread of shapes, walker counts, correlator counts and accumulations
+    rc, log = _compile(_cfg(n_slices=N, bisection_level=S, n_walkers=W, accum=accum),
+                       "0.5 * x1 * x1", "", ("x1 * x1",), tuple("x1" + " * x1" * k for k in range(ncor)))
+    assert rc == 0, log
+
+
 def test_lm2m2_plugin_compiles():
     from feynsimul_gb300.physical_systems.lm2m2 import Lm2m2Cluster
     s = Lm2m2Cluster(4, 0.5)

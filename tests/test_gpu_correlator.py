@@ -99,3 +99,26 @@ def test_pipelined_helpers_bit_identical(cors, accumulation):
     assert np.array_equal(kp._raw_correlator(), kh._raw_correlator())
     kp.close()
     kh.close()
+
+
+@pytest.mark.parametrize("N,S", [(32, 2), (64, 3), (64, 2), (128, 4), (256, 4)])
+def test_pipelined_helpers_bit_identical_across_shapes(N, S):
+    """Pipelined helpers (walkers per CTA filling whole warps of movers) against the same run
+    with one walker per CTA (helpers after the moves, or none): identical bits, IEEE build."""
+    require_gpu()
+    W, tpw = 64, N >> S
+    kp = _kernel("fp32", True, N, S, W, wpb=32 // tpw, fast=False)
+    kh = _kernel("fp32", True, N, S, W, wpb=1, fast=False)
+    groups = -(-(N // 8) // tpw)
+    assert kp._info.block_threads == (32 // tpw) * tpw * (1 + groups)
+    p0 = (np.random.RandomState(N + S).randn(W, N) * 0.7).astype(np.float32)
+    for k in (kp, kh):
+        k.setPaths(p0)
+    for _ in range(2):
+        kp.run()
+        kh.run()
+    assert np.array_equal(kp.getPaths(), kh.getPaths())
+    assert np.array_equal(kp._raw_operators(), kh._raw_operators())
+    assert np.array_equal(kp._raw_correlator(), kh._raw_correlator())
+    kp.close()
+    kh.close()
