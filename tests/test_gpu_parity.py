@@ -107,6 +107,10 @@ FIXED_CASES = {
     "xorshift_parallel:n4_s1": dict(N=4, S=1),
     "xorshift_parallel:n8_s3": dict(N=8, S=3),
     "xorshift_walker:n8": dict(N=8),
+    # a walker count no CTA shape divides (the last CTA holds inactive walkers), and walkers
+    # of more than 32 segment threads (one walker per CTA, block-wide barriers)
+    "xorshift_parallel:w13": dict(nbrOfWalkers=13, nbrOfWalkersPerWorkGroup=1),
+    "xorshift_parallel:n512_s2": dict(N=512, S=2, nbrOfWalkers=4, nbrOfWalkersPerWorkGroup=1),
 }
 
 
