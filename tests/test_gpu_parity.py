@@ -111,6 +111,8 @@ FIXED_CASES = {
     # of more than 32 segment threads (one walker per CTA, block-wide barriers)
     "xorshift_parallel:w13": dict(nbrOfWalkers=13, nbrOfWalkersPerWorkGroup=1),
     "xorshift_parallel:n512_s2": dict(N=512, S=2, nbrOfWalkers=4, nbrOfWalkersPerWorkGroup=1),
+    # the largest walker: 1024 segment threads, 4096 correlator lags of 8192 products
+    "xorshift_parallel:n8192_s3": dict(N=8192, S=3, nbrOfWalkers=2, nbrOfWalkersPerWorkGroup=1),
 }
 
 
