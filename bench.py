@@ -610,8 +610,9 @@ def run_gb300(args, rank, world):
     wpb = args.wpb if args.wpb > 0 else TUNED_WPB.get(args.config, 0)
     from feynsimul_gb300.replicas import ReplicaGroup, replica_seed
     group = ReplicaGroup()
+    pc = {"auto": None, "shared": True, "device": "device", "off": False}[args.potential_cache]
     ka_obj = KernelArgs(system=sysm, seed=replica_seed(1000, rank), walkersPerBlock=wpb,
-                        minBlocksPerSM=minb, **extra, **ka)
+                        minBlocksPerSM=minb, potentialCache=pc, **extra, **ka)
     k = PIMCKernel(ka_obj)
     paths0 = initial_paths(sysm, ka, replica_seed(17, rank))
     k.setPaths(paths0)
@@ -681,7 +682,7 @@ def run_gb300(args, rank, world):
         from feynsimul_gb300.learned import energy_ess
         ka_e = dict(ka, operatorRuns=1, metroStepsPerOperatorRun=1)
         ke = PIMCKernel(KernelArgs(system=sysm, seed=replica_seed(2000, rank), walkersPerBlock=wpb,
-                                   minBlocksPerSM=minb, **extra, **ka_e))
+                                   minBlocksPerSM=minb, potentialCache=pc, **extra, **ka_e))
         ke.setPaths(host_paths)
         if ka["enableRanlux"]:
             ke.initRanlux()
@@ -707,7 +708,8 @@ def run_gb300(args, rank, world):
         "config": bench_config(workload, ka),
         "timing": {"l2": "flushed between launches (512 MiB write)", "parallelism": f"replicas x{world}"},
         "launch": {"walkers_per_block": int(info.walkers_per_block), "registers": int(info.registers),
-                   "smem_bytes": int(info.smem_bytes), "grid": int(info.grid_blocks)},
+                   "smem_bytes": int(info.smem_bytes), "grid": int(info.grid_blocks),
+                   "potential_cache": {0: "none", 1: "shared", 3: "device"}.get(int(info.potential_cache))},
         "e2e": {"value": e2e_value, "unit": "node-updates/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "pinned": pinned, "api": "PIMCKernel.runHost + getOperators",
                 "chunks": k.lastChunks},
@@ -746,6 +748,8 @@ def main():
     ap.add_argument("--ess-launches", type=int, default=200, help="measurements per walker of the ESS loop")
     ap.add_argument("--no-batch", action="store_true", help="skip the ragged-batch sub-record of the default run")
     ap.add_argument("--no-ho", action="store_true", help="skip the harmonic-oscillator sub-record of the default run")
+    ap.add_argument("--potential-cache", default="auto", choices=["auto", "shared", "device", "off"],
+                    help="he3 / ho configs: where V of every slice is kept between moves (auto = the library's choice)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

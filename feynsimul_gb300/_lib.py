@@ -68,7 +68,7 @@ class FsConfig(ctypes.Structure):
 class FsInfo(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int64) for n in (
         "n_threads", "threads_per_walker", "walkers_per_block", "block_threads", "grid_blocks",
-        "smem_bytes", "registers", "device_bytes", "uniforms_per_move", "nodes_per_move")]
+        "smem_bytes", "registers", "device_bytes", "uniforms_per_move", "nodes_per_move", "potential_cache")]
 
 
 class FsBatchSystem(ctypes.Structure):

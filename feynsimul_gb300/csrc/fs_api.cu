@@ -73,6 +73,7 @@ struct fs_handle {
     long long cwstride = 0;  // per-walker correlator buffer in shared memory, elements
     int resident_per_sm = 0;  // resident CTAs per SM of the sweep kernel (fs_run_host), 0 = not yet queried
     long long wstride = 0, vstride = 0;
+    int vglobal = 0;  // potential cache in device memory (FS_VGLOBAL) instead of shared memory
     long long n_threads = 0;
     size_t smem = 0;
     int regs = 0;
@@ -80,6 +81,7 @@ struct fs_handle {
     size_t n_ops_elems = 0, n_cor_elems = 0, n_cor_lags = 0, n_bins = 0, n_hist = 0;
     double *d_red = nullptr;  // fs_reduce_correlator output (sum, sumsq)
     void *d_shift_old = nullptr;  // path shift, fixed mode: row saved before the move
+    void *d_vcache = nullptr;     // potential cache in device memory: [walkers][N]
     unsigned long long steps_done = 0;  // Metropolis steps of all launches so far
     int last_chunks = 0;                // chunks (kernel launches per sweep set) of the last fs_run_host
     // CUDA objects
@@ -324,7 +326,8 @@ static std::string gen_source(const fs_handle &h, const std::string &potential,
       << lit(c.beta / (double)c.n_slices) << "\n#define FS_OPNORM " << lit(opnorm)
       << "\n#define FS_BINS " << (c.enable_bins ? 1 : 0) << "\n#define FS_NHIST " << nhist
       << "\n#define FS_LEARNED " << (c.learned ? 1 : 0) << "\n#define FS_GLOBAL " << (c.global_path ? 1 : 0)
-      << "\n#define FS_VCACHE " << (h.vstride ? 1 : 0) << "\n#define FS_VSTRIDE " << h.vstride
+      << "\n#define FS_VCACHE " << (h.vstride || h.vglobal ? 1 : 0) << "\n#define FS_VSTRIDE " << h.vstride
+      << "\n#define FS_VGLOBAL " << h.vglobal
       << "\n#define FS_COR_ILV " << h.cor_ilv << "\n#define FS_CWSTRIDE " << h.cwstride << "\n#define FS_MX "
       << h.mx << "\n#define FS_PIPE " << h.pipe << "\n#define FS_SNSTRIDE " << h.snstride << "\n";
     {
@@ -562,6 +565,8 @@ static int validate(const fs_config &c, int nops, int ncor, int nhist)
     if (nhist > 0 && (c.hist_bins < 1 || c.hist_bins > 16384 || !(c.hist_hi > c.hist_lo)))
         return fail(nullptr, FS_ERR_CONFIG, "histogram needs 1..16384 bins and hist_lo < hist_hi");
     if (c.accum < 0 || c.accum > 3) return fail(nullptr, FS_ERR_CONFIG, "accum must be 0..3");
+    if (c.potential_cache < 0 || c.potential_cache > 3)
+        return fail(nullptr, FS_ERR_CONFIG, "potential_cache must be 0..3");
     if (c.partials != FS_PARTIALS_FP32 && c.partials != FS_PARTIALS_EXACT)
         return fail(nullptr, FS_ERR_CONFIG, "partials must be 0 (FP32) or 1 (exact)");
     if (nops < 0 || ncor < 0 || nops > 64 || ncor > 16)
@@ -592,7 +597,7 @@ static void free_buffers(fs_handle *h)
 {
     void *bufs[] = {h->d_paths, h->d_accepts, h->d_seeds, h->d_snap, h->d_wseeds, h->d_rtab,
                     h->d_gtab, h->d_bins, h->d_ops, h->d_cor, h->d_hist, h->d_status,
-                    h->d_mlp_frag, h->d_mlp_bias, h->d_red, h->d_shift_old, h->d_wops};
+                    h->d_mlp_frag, h->d_mlp_bias, h->d_red, h->d_shift_old, h->d_wops, h->d_vcache};
     for (void *p : bufs)
         if (p) cudaFree(p);
 }
@@ -702,7 +707,8 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     // the path-shift and single-node moves change slices outside the bisection's
     // bookkeeping, so they go without the potential cache
     const bool other_moves = (c.moves & (FS_MOVE_PATH_SHIFT | FS_MOVE_SINGLE_NODE)) != 0;
-    h->vstride = (c.potential_cache == 2 || other_moves) ? 0 : vstride;
+    h->vstride = (c.potential_cache == 2 || c.potential_cache == 3 || other_moves) ? 0 : vstride;
+    h->vglobal = c.potential_cache == 3 && !other_moves ? 1 : 0;
     size_t per_walker = per_walker_base + (size_t)h->vstride * h->ft;
     const size_t hist_bytes = (size_t)(c.hist_bins > 0 && !h->hists.empty() ? c.hist_bins : 0) * 4;
     if (c.walkers_per_block > 0) {
@@ -761,6 +767,12 @@ static int prepare(const fs_config *cfg, const char *potential, const char *user
     if (!h->vstride) {
         per_walker = per_walker_base;
         h->smem = per_walker * h->wpb + hist_bytes;
+        // automatic: where shared memory has no room for the cache, keep it in device memory
+        // (L1/L2), for potentials of 3 or more DOF and launches of more than one move; the
+        // launch starts with one potential evaluation per slice
+        if (c.potential_cache == 0 && !other_moves && c.dof >= 3 &&
+            (long long)c.operator_runs * c.metro_steps_per_operator_run >= 2)
+            h->vglobal = 1;
     }
     // Register budget: unless the caller fixes it, compile for as many CTAs per SM as shared
     // memory admits (<= 2048 threads per SM, >= 64 registers per thread) and as the grid can
@@ -899,6 +911,7 @@ extern "C" int fs_create(const fs_config *cfg, const char *potential, const char
     CREATE_TRY(dalloc(h, (void **)&h->d_hist, h->n_hist * 8));
     CREATE_TRY(dalloc(h, (void **)&h->d_status, 16));
     if ((c.moves & FS_MOVE_PATH_SHIFT) && !c.compat) CREATE_TRY(dalloc(h, &h->d_shift_old, W * N * h->ft));
+    if (h->vglobal) CREATE_TRY(dalloc(h, &h->d_vcache, W * N * h->ft));
     if (c.learned) {
         CREATE_TRY(dalloc(h, &h->d_mlp_frag, (size_t)FS_MLP_FRAG_BYTES));
         CREATE_TRY(dalloc(h, (void **)&h->d_mlp_bias, (size_t)FS_MLP_NBIAS_FLOATS * 4));
@@ -945,6 +958,7 @@ extern "C" int fs_query(const fs_handle *h, fs_info *info)
     info->device_bytes = (int64_t)h->device_bytes;
     info->nodes_per_move = h->seg - 1;
     info->uniforms_per_move = 2ll * h->cfg.dof * (h->seg - 1) + 1;
+    info->potential_cache = h->vglobal ? 3 : (h->vstride ? 1 : 0);
     return FS_OK;
 }
 
@@ -1066,6 +1080,7 @@ struct FsArgsHost {  // mirrors FsArgs in fs_pimc.cuh
     const float *mlp_bias;
     float mlp_inv_scale;
     int block_offset;
+    void *vcache;
 };
 
 extern "C" int fs_get_step_counter(fs_handle *h, uint64_t *steps)
@@ -1288,6 +1303,7 @@ static void fill_args(fs_handle *h, FsArgsHost &a)
     a.shift_old = h->d_shift_old;
     a.step_base = h->steps_done;
     a.block_offset = 0;
+    a.vcache = h->d_vcache;
 }
 
 // After the stream has drained: the status word the sweeps since the last check wrote

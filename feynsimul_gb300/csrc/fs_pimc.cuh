@@ -122,6 +122,18 @@
 #define FS_VCACHE 0
 #define FS_VSTRIDE 0
 #endif
+// The potential cache lives in shared memory (FS_VSTRIDE words per walker, the path's padded
+// slice layout) or, with FS_VGLOBAL, in device memory: N values per walker, slice s at
+// (s mod 2^S) * (N / 2^S) + s / 2^S, so the segment threads of a walker, whose slices lie
+// 2^S apart, touch consecutive words.  It costs no shared memory there, only L1/L2 traffic.
+#ifndef FS_VGLOBAL
+#define FS_VGLOBAL 0
+#endif
+#if FS_VGLOBAL
+#define FS_VIDX(s) ((((s) & (FS_SEG - 1)) * (FS_N / FS_SEG)) + ((s) >> FS_S))
+#else
+#define FS_VIDX(s) FS_PHYS(s)
+#endif
 
 #if FS_DOUBLE
 #define FS_ADD __dadd_rn
@@ -220,7 +232,7 @@ __device__ __forceinline__ fs_u32 fs_offset(FsIStream &g, fs_u32 range)
 // + [z_new^2 - ((x_old - lmu) / lsd)^2] / 2, with z_new the standard normal drawn.
 //
 // Potential cache (FS_VCACHE): Vc holds V(x_s) of every slice of the walker's current path
-// (same padded slice layout as the path).  The old action is then a sum of cached values
+// (FS_VIDX: shared or device memory).  The old action is then a sum of cached values
 // -- the same products and sums as evaluating V again, so bit for bit the same aOld --
 // and only the proposed nodes are evaluated; an accepted move leaves their new values in
 // the cache, a rejected one restores the path and re-evaluates its nodes.
@@ -236,15 +248,20 @@ __device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream 
 #pragma unroll
         for (int d = 0; d < FS_DOF; d++) old[(i - 1) * FS_DOF + d] = FS_AT(P, d, p);
     }
+#if FS_VCACHE
+    // cached values: the loads are independent, so they are issued together
+#pragma unroll 16
+    for (int i = 1; i < FS_SEG; i++) {
+        const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
+        aOld = FS_ADD(aOld, FS_MUL((FT)FS_EPS, Vc[FS_VIDX(p)]));
+    }
+#else
     FS_ACT_UNROLL
     for (int i = 1; i < FS_SEG; i++) {
         const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
-#if FS_VCACHE
-        aOld = FS_ADD(aOld, FS_MUL((FT)FS_EPS, Vc[FS_PHYS(p)]));
-#else
         aOld = FS_ADD(aOld, FS_MUL((FT)FS_EPS, fs_pot(FS_ARGS_AT(P, p))));
-#endif
     }
+#endif
     FS_MOVE_UNROLL
     for (int n = 1; n <= FS_S; n++) {
         const int half = 1 << (FS_S - n);
@@ -298,7 +315,7 @@ __device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream 
         const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
         const FT v = fs_pot(FS_ARGS_AT(P, p));
 #if FS_VCACHE
-        Vc[FS_PHYS(p)] = v;
+        Vc[FS_VIDX(p)] = v;
 #endif
         aNew = FS_ADD(aNew, FS_MUL((FT)FS_EPS, v));
     }
@@ -321,7 +338,7 @@ __device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream 
         FS_MOVE_UNROLL
         for (int i = 1; i < FS_SEG; i++) {
             const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
-            Vc[FS_PHYS(p)] = fs_pot(FS_ARGS_AT(P, p));
+            Vc[FS_VIDX(p)] = fs_pot(FS_ARGS_AT(P, p));
         }
 #else
         (void)Vc;
@@ -462,6 +479,7 @@ struct FsArgs {
     const float *mlp_bias;
     float mlp_inv_scale;       // features = endpoint coordinates * mlp_inv_scale
     int block_offset;          // first CTA of this launch (chunked launches of fs_run_host)
+    FT *vcache;                // potential cache in device memory (FS_VGLOBAL): [walkers][N]
 };
 
 __device__ __forceinline__ int fs_thread_id(int w, int t)
@@ -686,7 +704,11 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
 #else
         FT *P = s_path + wl * FS_WSTRIDE;
 #endif
+#if FS_VGLOBAL
+        FT *Vc = a.vcache + (size_t)w * FS_N;
+#else
         FT *Vc = s_v + wl * FS_VSTRIDE;
+#endif
         const int tid = fs_thread_id(w, t);
         // sigma table (kernel.c:608-618), computed on the host with the same FP operations
         const FT *sigma = fs_sigma;
@@ -772,7 +794,7 @@ extern "C" __global__ void FS_LAUNCH_BOUNDS fs_metropolis(FsArgs a)
             const int v_lo = 0, v_hi = FS_N;
 #endif
 #pragma unroll 1
-            for (int s = v_lo; s < (mover ? v_hi : v_lo); s++) Vc[FS_PHYS(s)] = fs_pot(FS_ARGS_AT(P, s));
+            for (int s = v_lo; s < (mover ? v_hi : v_lo); s++) Vc[FS_VIDX(s)] = fs_pot(FS_ARGS_AT(P, s));
         }
         FS_WSYNC();
 #endif

@@ -202,7 +202,9 @@ class PIMCKernel:
         # is per-thread private data either way (registers, spilling to local memory)
         c.global_path = int(bool(self._enableGlobalPath)) if self._enableBisection else 0
         pc = getattr(ka, "potentialCache", None)
-        c.potential_cache = 0 if pc is None else (1 if pc else 2)
+        if not (pc is None or isinstance(pc, bool) or pc == "device"):
+            raise ValueError("potentialCache must be None, True, False or 'device'")
+        c.potential_cache = 0 if pc is None else (3 if pc == "device" else (1 if pc else 2))
         c.moves = ((_lib.FS_MOVE_BISECTION if self._enableBisection else 0)
                    | (_lib.FS_MOVE_PATH_SHIFT if self._enablePathShift else 0)
                    | (_lib.FS_MOVE_SINGLE_NODE if self._enableSingleNodeMove else 0))

@@ -26,9 +26,10 @@ Keyword-only additions of this engine:
 * ``learnedProposal`` (False): draw each segment's level-1 midpoint from a learned Gaussian
   (feynsimul_gb300.learned), Metropolis-Hastings corrected; load the model with
   PIMCKernel.setLearnedProposal.
-* ``potentialCache`` (None = automatic): keep V of every slice in shared memory so a move
-  evaluates the potential only at its proposed nodes (bit-identical results; costs
-  shared memory, i.e. occupancy).
+* ``potentialCache`` (None = automatic): keep V of every slice between moves so a move
+  evaluates the potential only at its proposed nodes (bit-identical results): True = in
+  shared memory (costs occupancy), "device" = in device memory (N values per walker, L1/L2
+  resident), False = off.
 * ``seed`` (None): master seed for the seed tables; None draws from ``np.random`` exactly
   as kernel.py:412-426 does.
 """

@@ -106,9 +106,13 @@ typedef struct fs_config {
      * each walker in shared memory; for paths larger than shared memory (e.g. 27 DOF x
      * 1024 slices in FP64).  Same arithmetic and results as the shared-memory sweep. */
     int32_t global_path;
-    /* new: potential cache (V of every slice kept in shared memory, so a move evaluates the
-     * potential only at its proposed nodes): 0 = automatic, 1 = on, 2 = off.  Results are
-     * bit-identical either way; it trades shared memory (occupancy) for potential work. */
+    /* new: potential cache (V of every slice kept between moves, so a move evaluates the
+     * potential only at its proposed nodes): 0 = automatic, 1 = in shared memory, 2 = off,
+     * 3 = in device memory (N values per walker, L1/L2 resident).  Results are bit-identical
+     * either way; in shared memory it trades occupancy for potential work, in device memory
+     * cache traffic.  Automatic: shared memory where that costs no resident CTA per SM (or
+     * for more than 8 DOF), else device memory for 3 or more DOF and launches of more than
+     * one move, else none. */
     int32_t potential_cache;
     /* Move types per Metropolis step, walker mode (enable_parallelize_path = 0) for all but
      * the bisection: 0 = bisection only (the default); otherwise a mask of FS_MOVE_* --
@@ -146,6 +150,7 @@ typedef struct fs_info {
     int64_t device_bytes;       /* device memory held by the handle */
     int64_t uniforms_per_move;  /* 2 * DOF * (2^S - 1) + 1 */
     int64_t nodes_per_move;     /* 2^S - 1 */
+    int64_t potential_cache;    /* the potential cache in use: 0 none, 1 shared memory, 3 device memory */
 } fs_info;
 
 /* Build the sweep for one configuration: validates, generates the CUDA source from the

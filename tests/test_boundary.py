@@ -60,6 +60,9 @@ def _compile(cfg, pot, uc="", ops=(), cors=(), hists=()):
     dict(accum=2),                                          # Kahan operators, pipelined lags
     dict(accum=2, enable_parallelize_path=0, walkers_per_group=1),  # FMA partials, one lag loop
     dict(n_slices=2, bisection_level=1),                    # N not a multiple of 4
+    dict(potential_cache=3),                                # potential cache in device memory
+    dict(potential_cache=3, enable_parallelize_path=0, walkers_per_group=1, enable_ranlux=1),
+    dict(potential_cache=3, global_path=1, enable_double=1),
 ])
 def test_nvrtc_compiles_for_sm103a(kw):
     rc, log = _compile(_cfg(**kw), "0.5 * 1.0 * x1 * x1", "FLOAT_TYPE sqr(FLOAT_TYPE x){return x*x;}",
@@ -108,6 +111,7 @@ def test_compile_error_is_reported():
     (dict(bisection_level=9), "2^S"),
     (dict(n_walkers=10, walkers_per_group=4), "multiple"),
     (dict(enable_ranlux=1, luxury_factor=7), "luxuaryFactor"),
+    (dict(potential_cache=4), "potential_cache"),
 ])
 def test_config_errors(kw, msg):
     rc, log = _compile(_cfg(**kw), "x1")
