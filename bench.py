@@ -289,7 +289,7 @@ def alg_ops_per_node(config, ka):
 
 # DRAM bytes per fs_metropolis launch from one ncu capture of the default workload
 # (dram__bytes_read.sum + dram__bytes_write.sum; profiles/fs_metropolis_he3_lm2m2_ranlux.md)
-TRAFFIC_PER_LAUNCH = {"he3": 226.9e6}
+TRAFFIC_PER_LAUNCH = {"he3": 262.7e6}
 
 
 def roofline_for(config, ka, node_rate, clk, default_workload=True):
@@ -301,8 +301,12 @@ def roofline_for(config, ka, node_rate, clk, default_workload=True):
     return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Tlane-op/s",
             "frac": achieved / peak, "traffic": traffic,
             "traffic_unit": "DRAM bytes per launch (ncu), against the ~250 MB of paths, RANLUX tables and "
-                            "results a launch must move: the kernel is not memory bound",
+                            "results a launch must move, plus the 16 MB potential cache: the kernel is not "
+                            "memory bound",
             "alg_ops_per_node": per_node,
+            "alg_basis": "the reference algorithm's lane operations per node update: RANLUX or xorshift "
+                         "uniforms, Box-Muller, two potential evaluations (old and new action; with the "
+                         "potential cache the old one is a cached load) and the measurements",
             "peak_basis": f"4 x 32 x 152 lanes per clock at the sampled median SM clock {sm_mhz:.0f} MHz "
                           "(MEASURED_PEAKS.json has HBM and bf16 peaks only; this kernel uses neither)"}
 

@@ -134,6 +134,10 @@
 #else
 #define FS_VIDX(s) FS_PHYS(s)
 #endif
+// a move keeps its old cached values (FS_SEG - 1 of them) for a rejection
+#ifndef FS_VKEEP
+#define FS_VKEEP (FS_SEG <= 33)
+#endif
 
 #if FS_DOUBLE
 #define FS_ADD __dadd_rn
@@ -249,12 +253,25 @@ __device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream 
         for (int d = 0; d < FS_DOF; d++) old[(i - 1) * FS_DOF + d] = FS_AT(P, d, p);
     }
 #if FS_VCACHE
-    // cached values: the loads are independent, so they are issued together
+    // cached values: the loads are independent, so they are issued together; with at most
+    // 32 interior slices they are kept and written back if the move is rejected (a
+    // re-evaluation there would cost the warp the potential of every slice whenever one of
+    // its lanes rejects)
+#if FS_VKEEP
+    FT vold[FS_SEG - 1];
+#pragma unroll
+    for (int i = 1; i < FS_SEG; i++) {
+        const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
+        vold[i - 1] = Vc[FS_VIDX(p)];
+        aOld = FS_ADD(aOld, FS_MUL((FT)FS_EPS, vold[i - 1]));
+    }
+#else
 #pragma unroll 16
     for (int i = 1; i < FS_SEG; i++) {
         const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
         aOld = FS_ADD(aOld, FS_MUL((FT)FS_EPS, Vc[FS_VIDX(p)]));
     }
+#endif
 #else
     FS_ACT_UNROLL
     for (int i = 1; i < FS_SEG; i++) {
@@ -334,7 +351,10 @@ __device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream 
 #pragma unroll
             for (int d = 0; d < FS_DOF; d++) FS_AT(P, d, p) = old[(i - 1) * FS_DOF + d];
         }
-#if FS_VCACHE
+#if FS_VCACHE && FS_VKEEP
+#pragma unroll
+        for (int i = 1; i < FS_SEG; i++) Vc[FS_VIDX((start + (fs_u32)i) & (FS_N - 1))] = vold[i - 1];
+#elif FS_VCACHE
         FS_MOVE_UNROLL
         for (int i = 1; i < FS_SEG; i++) {
             const fs_u32 p = (start + (fs_u32)i) & (FS_N - 1);
