@@ -40,7 +40,9 @@ __device__ __forceinline__ fs_u32 fsb_offset(FsbStream &g, fs_u32 range) { retur
 
 struct FsBatchSys {
     float *paths;            // [walkers][DOF][N]
-    float *old_scratch;      // per CTA slot: saved segments [(seg-1)*DOF][tile threads]
+    float *old_scratch;      // per CTA slot: saved segments [(seg-1)*DOF][tile threads], then
+                             // with the potential cache their cached V [(seg-1)][tile threads]
+    float *vcache;           // potential cache: V of every slice [walkers][N] (3 or more DOF)
     fs_u32 *seeds;           // [threads][4]  (thread = walker * tpw + t)
     fs_u32 *wseeds;          // [walkers][4]
     fs_u32 *rtab;            // RANLUX: [threads][28] (the reference's table layout)
@@ -70,6 +72,12 @@ __device__ __forceinline__ void fs_walker_sync(int tpw, int wl)
 }
 
 // One tile: walkers [tile*wpb, ...) of system sd.  All threads of the CTA call it.
+// Systems of 3 or more DOF keep V of every slice in device memory between moves (as the
+// sweep's potential cache: slice s of a walker at (s mod 2^S) * (N / 2^S) + s / 2^S, so a
+// walker's segment threads touch consecutive words): the old action is a sum of cached
+// values, the same products and sums as evaluating V again, and a move evaluates V only at
+// its proposed nodes.  The old values are saved beside the old segment and written back if
+// the move is rejected.
 // GLOBAL: the walkers' paths stay in device memory (L1/L2) and are worked on in place, for
 // walkers too large to put enough of them in shared memory to fill the CTA (the same
 // arithmetic as the shared-memory tile, like the sweep's global-path mode).
@@ -90,6 +98,8 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
     // saved old segments: this CTA's slice of the global scratch, [(seg-1)*DOF][tile threads]
     float *s_old = sd.old_scratch + (size_t)blockIdx.x * old_slot_floats;
     double *s_op = (double *)(GLOBAL ? smem : smem + sd.wpb * wstride);  // [wpb][nops]
+    constexpr bool VC = DOF >= 3;
+    float *s_oldv = s_old + (size_t)(seg - 1) * DOF * nthr;  // [(seg-1)][tile threads]
 
 #define FSB_AT(P, d, s) (GLOBAL ? (P)[(d) * N + (s)] : (P)[(d) * dstride + (s) + ((s) >> S)])
     {
@@ -124,6 +134,18 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
             ws.x = g4.x; ws.y = g4.y; ws.z = g4.z; ws.w = g4.w;
 #endif
         }
+        float *Vc = VC ? sd.vcache + (size_t)w * N : nullptr;
+#define FSB_VIDX(s) ((((s) & (seg - 1)) * tpw) + ((s) >> S))
+        if (VC) {
+#pragma unroll 1
+            for (int s = t * seg; s < (t + 1) * seg; s++) {
+                float x[DOF];
+#pragma unroll
+                for (int d = 0; d < DOF; d++) x[d] = FSB_AT(P, d, s);
+                Vc[FSB_VIDX(s)] = Sys::pot(x);
+            }
+            fs_walker_sync(tpw, wl);
+        }
         fs_u32 n_acc = 0u;
         double opd[Sys::NOPS > 0 ? Sys::NOPS : 1];
 #pragma unroll
@@ -146,7 +168,15 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
                         x[d] = FSB_AT(P, d, p);
                         s_old[((i - 1) * DOF + d) * nthr + tid] = x[d];
                     }
-                    aOld = __fadd_rn(aOld, __fmul_rn(eps, Sys::pot(x)));
+                    if (!VC) aOld = __fadd_rn(aOld, __fmul_rn(eps, Sys::pot(x)));
+                }
+                if (VC) {
+#pragma unroll 4
+                    for (int i = 1; i < seg; i++) {
+                        const float v = Vc[FSB_VIDX((start + i) & (N - 1))];
+                        s_oldv[(i - 1) * nthr + tid] = v;
+                        aOld = __fadd_rn(aOld, __fmul_rn(eps, v));
+                    }
                 }
 #pragma unroll 1
                 for (int n = 1; n <= S; n++) {
@@ -176,7 +206,9 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
                     const int p = (start + i) & (N - 1);
 #pragma unroll
                     for (int d = 0; d < DOF; d++) x[d] = FSB_AT(P, d, p);
-                    aNew = __fadd_rn(aNew, __fmul_rn(eps, Sys::pot(x)));
+                    const float v = Sys::pot(x);
+                    if (VC) Vc[FSB_VIDX(p)] = v;
+                    aNew = __fadd_rn(aNew, __fmul_rn(eps, v));
                 }
                 if (__expf(__fsub_rn(aOld, aNew)) < fsb_uniform(g)) {
 #pragma unroll 1
@@ -184,6 +216,7 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
                         const int p = (start + i) & (N - 1);
 #pragma unroll
                         for (int d = 0; d < DOF; d++) FSB_AT(P, d, p) = s_old[((i - 1) * DOF + d) * nthr + tid];
+                        if (VC) Vc[FSB_VIDX(p)] = s_oldv[(i - 1) * nthr + tid];
                     }
                 } else {
                     n_acc++;
@@ -236,5 +269,6 @@ __device__ __forceinline__ void fs_batch_tile(const FsBatchSys &sd, int tile, fl
         for (int i = tid; i < n_here * sd.nops; i += blockDim.x) sd.op_sums[(size_t)w0 * sd.nops + i] += s_op[i];
     }
     __syncthreads();  // the next tile reuses the shared-memory tile
+#undef FSB_VIDX
 #undef FSB_AT
 }

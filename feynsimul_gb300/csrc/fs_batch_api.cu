@@ -29,6 +29,7 @@ int fsi_compile(const std::string &src, bool fast, std::string *cubin, std::stri
 struct FsBatchSysHost {  // mirrors FsBatchSys in fs_batch.cuh
     float *paths;
     float *old_scratch;
+    float *vcache;
     uint32_t *seeds, *wseeds, *rtab, *gtab, *accepts;
     double *op_sums;
     int n_walkers, N, S, tpw, wpb, nops, type, n_tiles;
@@ -189,7 +190,8 @@ extern "C" int fs_batch_create(int32_t n_types, const int32_t *type_dof, const c
         s.walkers_per_tile = wpb;
         max_smem = std::max(max_smem, tile_bytes);
         const size_t seg = (size_t)1 << s.bisection_level;
-        max_old = std::max(max_old, (seg - 1) * dof * (size_t)(wpb * tpw));
+        // saved segment, and with the potential cache (3 or more DOF) its cached values
+        max_old = std::max(max_old, (seg - 1) * (dof + (dof >= 3 ? 1 : 0)) * (size_t)(wpb * tpw));
         b->node_updates += (long long)s.n_walkers * tpw * (long long)(seg - 1) * op_runs * msteps;
     }
     b->smem = max_smem;
@@ -322,6 +324,9 @@ extern "C" int fs_batch_create(int32_t n_types, const int32_t *type_dof, const c
         const size_t W = s.n_walkers, T = W * d.tpw;
         void *p;
         CT(balloc(b, &p, W * dof * s.n_slices * 4)); d.paths = (float *)p;
+        if (dof >= 3) {
+            CT(balloc(b, &p, W * s.n_slices * 4)); d.vcache = (float *)p;  // potential cache
+        }
         CT(balloc(b, &p, T * 16)); d.seeds = (uint32_t *)p;
         CT(balloc(b, &p, W * 16)); d.wseeds = (uint32_t *)p;
         if (b->lux >= 0) {
