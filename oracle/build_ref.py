@@ -174,7 +174,9 @@ def capture(ka_kwargs: dict, system, np_seed: int):
 def _compile(tag_text: str, c_text: str, name: str, single_constants: bool = True) -> str:
     os.makedirs(REF_BUILD, exist_ok=True)
     flags = [f for f in CFLAGS if single_constants or f != "-fsingle-precision-constant"]
-    h = hashlib.sha1((tag_text + c_text + " ".join(flags)).encode()).hexdigest()[:16]
+    with open(os.path.join(HERE, "cl_shim.h")) as f:
+        shim = f.read()
+    h = hashlib.sha1((tag_text + c_text + " ".join(flags) + shim).encode()).hexdigest()[:16]
     so = os.path.join(REF_BUILD, f"{name}_{h}.so")
     if os.path.exists(so):
         return so
@@ -233,6 +235,37 @@ int clsh_launch(int which, void **a, size_t g0, size_t g1, size_t l0, size_t l1)
 """
 
 
+def kernel_buffers(k):
+    """The metropolis kernel's buffers in argument order (the reference kernel's own numpy
+    arrays behind kernel.py's stub buffers), the C casts of the launcher's argument list, and
+    the launcher cases of the RANLUX initialisation kernels."""
+    ft = "double" if k._enableDouble else "float"
+    args = []
+
+    def add(cast):
+        args.append(f"({cast})a[{len(args)}]")
+
+    bufs = [k._paths, k._accepts]
+    add(f"{ft} *"); add("uint *")
+    if not k._enableRanlux:
+        bufs.append(k._seeds); add("uint *")
+    if k._enableGlobalOldPath:
+        bufs.append(k._oldPath); add(f"{ft} *")
+    if k._enableOperator:
+        bufs.append(k._operatorValues); add(f"{ft} *")
+    if k._enableCorrelator:
+        bufs.append(k._correlatorValues); add(f"{ft} *")
+    if k._enableBins:
+        bufs.append(k._binCounts); add("uint *")
+    ranlux_cases = ""
+    if k._enableRanlux:
+        bufs += [k._ranluxcltab, k._groupRanluxcltab]
+        add("ranluxcl_state_t *"); add("ranluxcl_state_t *")
+        ranlux_cases = ("    case 1: ranlux_init_kernel((uint *)a[0], (ranluxcl_state_t *)a[1]); break;\n"
+                        "    case 2: ranlux_group_init_kernel((uint *)a[0], (ranluxcl_state_t *)a[1]); break;\n")
+    return bufs, args, ranlux_cases
+
+
 class RefKernel:
     """The reference's metropolis kernel, compiled for the CPU, behind kernel.py's buffers."""
 
@@ -253,30 +286,7 @@ class RefKernel:
             self.l = (1, 1)
         else:
             self.l = cap["local_size"]
-        ft = "double" if k._enableDouble else "float"
-        args, ctypes_args = [], []
-
-        def add(cast):
-            args.append(f"({cast})a[{len(args)}]")
-
-        self.bufs = [k._paths, k._accepts]
-        add(f"{ft} *"); add("uint *")
-        if not k._enableRanlux:
-            self.bufs.append(k._seeds); add("uint *")
-        if k._enableGlobalOldPath:
-            self.bufs.append(k._oldPath); add(f"{ft} *")
-        if k._enableOperator:
-            self.bufs.append(k._operatorValues); add(f"{ft} *")
-        if k._enableCorrelator:
-            self.bufs.append(k._correlatorValues); add(f"{ft} *")
-        if k._enableBins:
-            self.bufs.append(k._binCounts); add("uint *")
-        ranlux_cases = ""
-        if k._enableRanlux:
-            self.bufs += [k._ranluxcltab, k._groupRanluxcltab]
-            add("ranluxcl_state_t *"); add("ranluxcl_state_t *")
-            ranlux_cases = ("    case 1: ranlux_init_kernel((uint *)a[0], (ranluxcl_state_t *)a[1]); break;\n"
-                            "    case 2: ranlux_group_init_kernel((uint *)a[0], (ranluxcl_state_t *)a[1]); break;\n")
+        self.bufs, args, ranlux_cases = kernel_buffers(k)
         src = cap["source"].replace(SWIZZLE, SWIZZLE_C)
         launcher = _LAUNCHER % {"METRO_ARGS": ", ".join(args), "RANLUX_CASES": ranlux_cases}
         c_text = ('#include "cl_shim.h"\n#include <stdlib.h>\n' + src + "\n" + launcher)

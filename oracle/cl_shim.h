@@ -58,7 +58,21 @@ static inline size_t get_local_id(uint d) { return d < 3 ? clsh_item.lid[d] : 0;
 static inline size_t get_group_id(uint d) { return d < 3 ? clsh_item.grp[d] : 0; }
 static inline size_t get_global_size(uint d) { return d < 3 ? clsh_item.gsz[d] : 1; }
 static inline size_t get_local_size(uint d) { return d < 3 ? clsh_item.lsz[d] : 1; }
-static inline void barrier(int flags) { (void)flags; pthread_barrier_wait(clsh_barrier); }
+/* Fiber launches (oracle/ref_timing.py): the work-items of one work-group run as fibers on
+ * one OS thread, and barrier() hands over to the group's next fiber through this hook. */
+static _Thread_local void (*clsh_barrier_hook)(void);
+static inline void barrier(int flags)
+{
+    (void)flags;
+    if (clsh_barrier_hook)
+        clsh_barrier_hook();
+    else
+        pthread_barrier_wait(clsh_barrier);
+}
+/* OpenCL built-ins that plugin code may call (type-generic through tgmath's sqrt) */
+#ifndef rsqrt
+#define rsqrt(x) (1 / sqrt(x))
+#endif
 static inline uint atom_inc(volatile uint *p) { return __atomic_fetch_add(p, 1u, __ATOMIC_RELAXED); }
 
 #endif

@@ -46,6 +46,28 @@ def test_cpu_baseline_keeps_the_measurement_cadence():
     assert "one measurement every 1 sweep(s)" in cb["sample"]
 
 
+def test_reference_rate_falls_back_to_the_restatement():
+    # the harmonic oscillator, and a configuration other than the prepared sample's, are timed
+    # with the oracle's restatement, saying why
+    sysm, ka, extra, _ = bench.ho_setup()
+    cb = bench.reference_cpu_rate("ho", sysm, dict(ka, nbrOfWalkers=8), extra, seconds=0.2)
+    assert cb["kind"] == "port" and cb["value"] > 0 and cb["reference_unavailable"]
+    sysm, ka, extra, _ = bench.he3_setup(walkers=8, S=3)
+    cb = bench.reference_cpu_rate("he3", sysm, ka, extra, seconds=0.2)
+    assert cb["kind"] == "port" and cb["reference_unavailable"]
+
+
+def test_reference_rate_times_the_prepared_reference_sample():
+    import pytest
+    from oracle import ref_timing
+    if not ref_timing.available("he3"):
+        pytest.skip("no prepared reference sample (the reference tree was absent at build time)")
+    sysm, ka, extra, _ = bench.he3_setup()
+    cb = bench.reference_cpu_rate("he3", sysm, ka, extra, seconds=0.5)
+    assert cb["kind"] == "reference" and cb["value"] > 0, cb
+    assert "reference_unavailable" not in cb
+
+
 def test_batch_cpu_baseline_weights_systems_by_their_work():
     from feynsimul_gb300.batch import choose_S, ragged_workload
     from feynsimul_gb300.physical_systems.lm2m2 import Lm2m2Cluster
