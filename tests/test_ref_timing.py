@@ -49,6 +49,32 @@ def test_fiber_work_groups_match_thread_per_work_item():
     assert rk.k._accepts.arr.sum() > 0
 
 
+def test_fiber_work_groups_with_the_correlators_barriers():
+    """The harmonic oscillator with its correlator: a work-group barrier per lag and slice
+    (kernel.c:792), 2 walkers per work group; fibers against one thread per work-item."""
+    import types
+    from oracle import ref_timing
+    sysm = types.SimpleNamespace(DOF=1, potential="0.5*x1*x1", userCode="")
+
+    def ka(global_path):
+        return dict(nbrOfWalkers=4, N=16, beta=4.0, S=2, enableOperator=True, enableCorrelator=True,
+                    enableBisection=True, enablePathShift=False, enableSingleNodeMove=False, enableBins=False,
+                    nbrOfWalkersPerWorkGroup=2, enableParallelizePath=True, enableGlobalPath=global_path,
+                    enableGlobalOldPath=False, enableDouble=False, enableRanlux=False,
+                    operators=("x1*x1",), correlators=("x1",), operatorRuns=3, metroStepsPerOperatorRun=2)
+    ref_timing.prepare("test_ho", sysm, ka(False))
+    fk = ref_timing.FiberKernel("test_ho", fast=False)
+    rk = build_ref.RefKernel(ka(True), sysm, np_seed=0)
+    p0 = (np.random.RandomState(8).randn(4, 16) * 0.5).astype(np.float32)
+    fk.set_paths(p0)
+    rk.set_paths(p0)
+    fk.run(2)
+    rk.run()
+    for i, b in enumerate(rk.bufs):   # paths, accepts, seed rows, operator and correlator sums
+        assert np.array_equal(fk.bufs[i], b.arr), i
+    assert rk.k._accepts.arr.sum() > 0
+
+
 def test_rate_of_a_prepared_sample():
     from oracle import ref_timing
     sysm, ka = _he3_ka(False, walkers=8)
