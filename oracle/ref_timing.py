@@ -234,11 +234,12 @@ class FiberKernel:
         tag = hashlib.sha1((c_text + " ".join(flags)).encode()).hexdigest()[:16]
         so = os.path.join(REF_BUILD, f"timing_{name}_{platform.machine()}_{tag}.so")
         if not os.path.exists(so):
-            r = subprocess.run(["gcc", *flags, src, "-o", so + ".tmp", "-lpthread", "-lm"],
+            tmp = f"{so}.{os.getpid()}.tmp"     # concurrent builds each write their own file
+            r = subprocess.run(["gcc", *flags, src, "-o", tmp, "-lpthread", "-lm"],
                                capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError("reference timing build failed:\n" + r.stderr[-3000:])
-            os.replace(so + ".tmp", so)
+            os.replace(tmp, so)
         self.lib = ctypes.CDLL(so)
         self.lib.clsh_launch_groups.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t,
                                                 ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int]
