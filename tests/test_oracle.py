@@ -105,6 +105,51 @@ def test_oracle_against_live_reference():
     assert np.array_equal(o.paths, r.k._paths.arr)
 
 
+def test_oracle_against_live_reference_he3_bench_configuration():
+    """The benchmarked configuration's arithmetic against the reference's own kernel: the He3
+    trimer plugin, RANLUX luxuaryFactor 2, parallel-path mode with the path in __local
+    memory (the reference kernel run with its work-groups as fibers, oracle/ref_timing.py,
+    IEEE flags), N = 256, S = 4, 4 walkers, 2 launches; the oracle in the reference's
+    compatible mode on the same RANLUX tables: tables, accept counts, paths and operator sums
+    bit-exact (both sides call the same C library)."""
+    from oracle import build_ref as br
+    if not br.reference_available():
+        pytest.skip("reference tree not present")
+    from feynsimul_gb300.physical_systems.lm2m2 import Lm2m2Cluster
+    from oracle import ref_timing
+    from oracle.oracle import OracleConfig, OracleSampler
+    sysm = Lm2m2Cluster(3, 1.0)
+    ka = dict(nbrOfWalkers=4, N=256, beta=float(sysm.beta), S=4, enableOperator=True,
+              enableCorrelator=False, enableBisection=True, enablePathShift=False,
+              enableSingleNodeMove=False, enableBins=False, nbrOfWalkersPerWorkGroup=1,
+              enableParallelizePath=True, enableGlobalPath=False, enableGlobalOldPath=False,
+              enableDouble=False, enableRanlux=True, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
+              operators=(sysm.energyOp,), operatorRuns=2, metroStepsPerOperatorRun=3)
+    ref_timing.prepare("test_he3_bench", sysm, ka)
+    fk = ref_timing.FiberKernel("test_he3_bench", fast=False)
+    o = OracleSampler(OracleConfig(
+        DOF=sysm.DOF, potential=sysm.potential, userCode=sysm.userCode, nbrOfWalkers=4, N=256,
+        beta=ka["beta"], S=4, operatorRuns=2, metroStepsPerOperatorRun=3, nbrOfWalkersPerWorkGroup=1,
+        enableParallelizePath=True, enableRanlux=True, luxuaryFactor=2, ranluxIntMax=2 ** 32 - 1,
+        operators=(sysm.energyOp,), compat=True, accum=0))
+    fk.init_ranlux(2)
+    o.ranlux_tab[...] = fk.bufs[-2].reshape(o.ranlux_tab.shape)
+    o.group_tab[...] = fk.bufs[-1].reshape(o.group_tab.shape)
+    p0 = sysm.initial_paths(4, 256, np.random.RandomState(12)).astype(np.float32)
+    fk.set_paths(p0)
+    o.paths[...] = p0.reshape(o.paths.shape)
+    for _ in range(2):
+        fk.run(2)
+        o.run()
+        assert np.array_equal(_masked(o.ranlux_tab), _masked(fk.bufs[-2]))
+        assert np.array_equal(_masked(o.group_tab), _masked(fk.bufs[-1]))
+        assert np.array_equal(o.accepts.reshape(-1), fk.bufs[1].reshape(-1))
+        assert np.array_equal(o.paths.reshape(-1), fk.bufs[0].reshape(-1))
+        ops = fk.bufs[2].reshape(-1)
+        assert np.array_equal(o.op_means.reshape(-1)[:ops.size], ops)
+    assert fk.bufs[1].sum() > 0
+
+
 @pytest.mark.parametrize("case", ["xorshift_walker", "xorshift_parallel"])
 def test_oracle_study_correlator_columns(case):
     """Precision-study accumulation sums the same products three ways on one trajectory:
