@@ -19,6 +19,11 @@ rate(name, seconds, threads) -- wherever those files are, the reference tree not
   work-groups: the work-items of one group as fibers (ucontext) on one OS thread, handing
   over at every barrier(), the groups spread over the host threads.
 
+In the xorshift mode the reference's work-items read a shared offset-seed row at their start
+and write it at their end (kernel.c:568-572, :832-835), so work-groups that run one after
+another see each other's writes, as they may on an OpenCL device; only RANLUX samples are
+timed, and the tests compare xorshift runs of one work-group.
+
 Two textual changes are applied to the generated text, never to the reference's files: the
 OpenCL swizzle of build_ref.SWIZZLE, and the parallel-path mode's __local path array
 (kernel.c:588-589), declared a thread-local static so that the fibers of a group, which

@@ -150,6 +150,49 @@ def test_oracle_against_live_reference_he3_bench_configuration():
     assert fk.bufs[1].sum() > 0
 
 
+def test_oracle_against_live_reference_ho_bench_configuration():
+    """The harmonic oscillator's benchmarked configuration against the reference's own kernel:
+    xorshift, N = 128, S = 3, the path in __local memory (work-groups as fibers), x^2 and the
+    correlator every sweep (a work-group barrier per lag and slice, kernel.c:792), 2 launches
+    of 3 sweeps; the oracle in the reference-compatible mode on the same seed table: seed
+    rows, accept counts, paths, operator and correlator sums bit-exact.  One walker, i.e. one
+    work-group: every work-item reads the shared offset-seed row at its start and writes it
+    at its end (kernel.c:568-572, :832-835), so work-groups that run one after another see
+    each other's writes, which the oracle's all-read-then-all-write order does not model."""
+    from oracle import build_ref as br
+    if not br.reference_available():
+        pytest.skip("reference tree not present")
+    from feynsimul_gb300.physical_systems.harm_osc import HarmOsc
+    from oracle import ref_timing
+    from oracle.oracle import OracleConfig, OracleSampler
+    sysm = HarmOsc()
+    ka = dict(nbrOfWalkers=1, N=128, beta=10.0, S=3, enableOperator=True, enableCorrelator=True,
+              enableBisection=True, enablePathShift=False, enableSingleNodeMove=False, enableBins=False,
+              nbrOfWalkersPerWorkGroup=1, enableParallelizePath=True, enableGlobalPath=False,
+              enableGlobalOldPath=False, enableDouble=False, enableRanlux=False,
+              operators=(sysm.energyOp,), correlators=("x1",), operatorRuns=3, metroStepsPerOperatorRun=1)
+    ref_timing.prepare("test_ho_bench", sysm, ka)
+    fk = ref_timing.FiberKernel("test_ho_bench", fast=False)
+    o = OracleSampler(OracleConfig(
+        DOF=1, potential=sysm.potential, userCode=sysm.userCode, nbrOfWalkers=1, N=128, beta=10.0, S=3,
+        operatorRuns=3, metroStepsPerOperatorRun=1, nbrOfWalkersPerWorkGroup=1, enableParallelizePath=True,
+        operators=(sysm.energyOp,), correlators=("x1",), compat=True, accum=0))
+    paths, accepts, seeds, ops, cors = fk.bufs
+    o.seeds[...] = seeds.reshape(o.seeds.shape)
+    p0 = (np.random.RandomState(13).randn(1, 128) * 0.6).astype(np.float32)
+    fk.set_paths(p0)
+    o.paths[...] = p0.reshape(o.paths.shape)
+    for _ in range(2):
+        fk.run(2)
+        o.run()
+        assert np.array_equal(o.seeds.reshape(-1), seeds.reshape(-1))
+        assert np.array_equal(o.accepts.reshape(-1), accepts.reshape(-1))
+        assert np.array_equal(o.paths.reshape(-1), paths.reshape(-1))
+        assert np.array_equal(o.op_means.reshape(-1)[:ops.size], ops.reshape(-1))
+        assert np.array_equal(o.cor_means.reshape(-1), cors.reshape(-1))
+    assert accepts.sum() > 0
+
+
 @pytest.mark.parametrize("case", ["xorshift_walker", "xorshift_parallel"])
 def test_oracle_study_correlator_columns(case):
     """Precision-study accumulation sums the same products three ways on one trajectory:

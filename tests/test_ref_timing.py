@@ -51,13 +51,16 @@ def test_fiber_work_groups_match_thread_per_work_item():
 
 def test_fiber_work_groups_with_the_correlators_barriers():
     """The harmonic oscillator with its correlator: a work-group barrier per lag and slice
-    (kernel.c:792), 2 walkers per work group; fibers against one thread per work-item."""
+    (kernel.c:792), 2 walkers in one work group; fibers against one thread per work-item.
+    One work-group: in this xorshift mode every work-item reads the shared offset-seed row at
+    its start and writes it at its end (kernel.c:568-572, :832-835), so work-groups that run
+    one after another see each other's writes and the launch order would matter."""
     import types
     from oracle import ref_timing
     sysm = types.SimpleNamespace(DOF=1, potential="0.5*x1*x1", userCode="")
 
     def ka(global_path):
-        return dict(nbrOfWalkers=4, N=16, beta=4.0, S=2, enableOperator=True, enableCorrelator=True,
+        return dict(nbrOfWalkers=2, N=16, beta=4.0, S=2, enableOperator=True, enableCorrelator=True,
                     enableBisection=True, enablePathShift=False, enableSingleNodeMove=False, enableBins=False,
                     nbrOfWalkersPerWorkGroup=2, enableParallelizePath=True, enableGlobalPath=global_path,
                     enableGlobalOldPath=False, enableDouble=False, enableRanlux=False,
@@ -65,7 +68,7 @@ def test_fiber_work_groups_with_the_correlators_barriers():
     ref_timing.prepare("test_ho", sysm, ka(False))
     fk = ref_timing.FiberKernel("test_ho", fast=False)
     rk = build_ref.RefKernel(ka(True), sysm, np_seed=0)
-    p0 = (np.random.RandomState(8).randn(4, 16) * 0.5).astype(np.float32)
+    p0 = (np.random.RandomState(8).randn(2, 16) * 0.5).astype(np.float32)
     fk.set_paths(p0)
     rk.set_paths(p0)
     fk.run(2)
