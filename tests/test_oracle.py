@@ -150,6 +150,51 @@ def test_oracle_against_live_reference_he3_bench_configuration():
     assert fk.bufs[1].sum() > 0
 
 
+@pytest.mark.parametrize("n,global_path", [(10, True), (5, False)], ids=["10_atoms_global", "5_atoms_local"])
+def test_oracle_against_live_reference_large_clusters(n, global_path):
+    """Larger clusters of the generated LM2M2 plugin (the precision study's 10 atoms, 27 DOF,
+    45 pairs, global paths; 5 atoms with the path in __local memory) against the reference's
+    own kernel (work-groups as fibers, IEEE flags), RANLUX, 2 launches: tables, accepts,
+    paths and operator sums bit-exact with the oracle in the reference-compatible mode."""
+    from oracle import build_ref as br
+    if not br.reference_available():
+        pytest.skip("reference tree not present")
+    from feynsimul_gb300.physical_systems.lm2m2 import Lm2m2Cluster
+    from oracle import ref_timing
+    from oracle.oracle import OracleConfig, OracleSampler
+    sysm = Lm2m2Cluster(n, 0.7)
+    W, N, S = 2, 32, 2
+    ka = dict(nbrOfWalkers=W, N=N, beta=float(sysm.beta), S=S, enableOperator=True,
+              enableCorrelator=False, enableBisection=True, enablePathShift=False,
+              enableSingleNodeMove=False, enableBins=False, nbrOfWalkersPerWorkGroup=1,
+              enableParallelizePath=True, enableGlobalPath=global_path, enableGlobalOldPath=False,
+              enableDouble=False, enableRanlux=True, luxuaryFactor=1, ranluxIntMax=2 ** 32 - 1,
+              operators=(sysm.energyOp, sysm.meanSquaredRadiusOp), operatorRuns=2, metroStepsPerOperatorRun=2)
+    name = f"test_cluster{n}"
+    ref_timing.prepare(name, sysm, ka)
+    fk = ref_timing.FiberKernel(name, fast=False)
+    o = OracleSampler(OracleConfig(
+        DOF=sysm.DOF, potential=sysm.potential, userCode=sysm.userCode, nbrOfWalkers=W, N=N,
+        beta=ka["beta"], S=S, operatorRuns=2, metroStepsPerOperatorRun=2, nbrOfWalkersPerWorkGroup=1,
+        enableParallelizePath=True, enableRanlux=True, luxuaryFactor=1, ranluxIntMax=2 ** 32 - 1,
+        operators=(sysm.energyOp, sysm.meanSquaredRadiusOp), compat=True, accum=0))
+    fk.init_ranlux(2)
+    o.ranlux_tab[...] = fk.bufs[-2].reshape(o.ranlux_tab.shape)
+    o.group_tab[...] = fk.bufs[-1].reshape(o.group_tab.shape)
+    p0 = sysm.initial_paths(W, N, np.random.RandomState(n)).astype(np.float32)
+    fk.set_paths(p0)
+    o.paths[...] = p0.reshape(o.paths.shape)
+    for _ in range(2):
+        fk.run(2)
+        o.run()
+        assert np.array_equal(_masked(o.ranlux_tab), _masked(fk.bufs[-2]))
+        assert np.array_equal(o.accepts.reshape(-1), fk.bufs[1].reshape(-1))
+        assert np.array_equal(o.paths.reshape(-1), fk.bufs[0].reshape(-1))
+        ops = fk.bufs[2].reshape(-1)
+        assert np.array_equal(o.op_means.reshape(-1)[:ops.size], ops)
+    assert fk.bufs[1].sum() > 0
+
+
 def test_oracle_against_live_reference_ho_bench_configuration():
     """The harmonic oscillator's benchmarked configuration against the reference's own kernel:
     xorshift, N = 128, S = 3, the path in __local memory (work-groups as fibers), x^2 and the
