@@ -239,7 +239,8 @@ __device__ __forceinline__ fs_u32 fs_offset(FsIStream &g, fs_u32 range)
 // (FS_VIDX: shared or device memory).  The old action is then a sum of cached values
 // -- the same products and sums as evaluating V again, so bit for bit the same aOld --
 // and only the proposed nodes are evaluated; an accepted move leaves their new values in
-// the cache, a rejected one restores the path and re-evaluates its nodes.
+// the cache, a rejected one restores the path and writes the kept old values back
+// (FS_VKEEP), or re-evaluates its nodes.
 __device__ __forceinline__ int fs_bisect(FT *P, FT *Vc, fs_u32 start, FsUStream &g, const FT *sigma,
                                          const FT *lmu, const FT *lsd)
 {
