@@ -168,3 +168,30 @@ def test_c_caller_links_and_compiles_a_sweep(tmp_path):
     env = dict(os.environ, FS_CACHE_DIR=str(tmp_path / "cache"))
     r = subprocess.run([exe], capture_output=True, text=True, env=env, timeout=300)
     assert r.returncode == 0 and "abi ok" in r.stdout, r.stdout + r.stderr
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """The Python mirrors of the C ABI's structs (feynsimul_gb300/_lib.py) have the header's
+    size and member offsets (tests/c/abi_layout.c prints them as the C compiler lays them out)."""
+    import shutil
+    import subprocess
+    L = _lib()
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    exe = str(tmp_path / "abi_layout")
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "c", "abi_layout.c"), "-o", exe], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    mirrors = {"fs_config": L.FsConfig, "fs_info": L.FsInfo, "fs_batch_system": L.FsBatchSystem}
+    seen = {k: set() for k in mirrors}
+    for line in filter(None, out):
+        struct, member, value = line.split()
+        cls = mirrors[struct]
+        if member == "sizeof":
+            assert ctypes.sizeof(cls) == int(value), struct
+        else:
+            assert getattr(cls, member).offset == int(value), (struct, member)
+            seen[struct].add(member)
+    for struct, cls in mirrors.items():
+        assert seen[struct] == {f[0] for f in cls._fields_}, struct   # every member, both sides
