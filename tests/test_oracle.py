@@ -150,12 +150,14 @@ def test_oracle_against_live_reference_he3_bench_configuration():
     assert fk.bufs[1].sum() > 0
 
 
-@pytest.mark.parametrize("n,global_path", [(10, True), (5, False)], ids=["10_atoms_global", "5_atoms_local"])
-def test_oracle_against_live_reference_large_clusters(n, global_path):
+@pytest.mark.parametrize("n,global_path,double", [(10, True, False), (5, False, False), (10, True, True)],
+                         ids=["10_atoms_global", "5_atoms_local", "10_atoms_global_fp64"])
+def test_oracle_against_live_reference_large_clusters(n, global_path, double):
     """Larger clusters of the generated LM2M2 plugin (the precision study's 10 atoms, 27 DOF,
-    45 pairs, global paths; 5 atoms with the path in __local memory) against the reference's
-    own kernel (work-groups as fibers, IEEE flags), RANLUX, 2 launches: tables, accepts,
-    paths and operator sums bit-exact with the oracle in the reference-compatible mode."""
+    45 pairs, global paths, also in the reference's FP64 build; 5 atoms with the path in
+    __local memory) against the reference's own kernel (work-groups as fibers, IEEE flags),
+    RANLUX, 2 launches: tables, accepts, paths and operator sums bit-exact with the oracle in
+    the reference-compatible mode."""
     from oracle import build_ref as br
     if not br.reference_available():
         pytest.skip("reference tree not present")
@@ -168,20 +170,20 @@ def test_oracle_against_live_reference_large_clusters(n, global_path):
               enableCorrelator=False, enableBisection=True, enablePathShift=False,
               enableSingleNodeMove=False, enableBins=False, nbrOfWalkersPerWorkGroup=1,
               enableParallelizePath=True, enableGlobalPath=global_path, enableGlobalOldPath=False,
-              enableDouble=False, enableRanlux=True, luxuaryFactor=1, ranluxIntMax=2 ** 32 - 1,
+              enableDouble=double, enableRanlux=True, luxuaryFactor=1, ranluxIntMax=2 ** 32 - 1,
               operators=(sysm.energyOp, sysm.meanSquaredRadiusOp), operatorRuns=2, metroStepsPerOperatorRun=2)
-    name = f"test_cluster{n}"
+    name = f"test_cluster{n}{'_fp64' if double else ''}"
     ref_timing.prepare(name, sysm, ka)
     fk = ref_timing.FiberKernel(name, fast=False)
     o = OracleSampler(OracleConfig(
         DOF=sysm.DOF, potential=sysm.potential, userCode=sysm.userCode, nbrOfWalkers=W, N=N,
         beta=ka["beta"], S=S, operatorRuns=2, metroStepsPerOperatorRun=2, nbrOfWalkersPerWorkGroup=1,
         enableParallelizePath=True, enableRanlux=True, luxuaryFactor=1, ranluxIntMax=2 ** 32 - 1,
-        operators=(sysm.energyOp, sysm.meanSquaredRadiusOp), compat=True, accum=0))
+        enableDouble=double, operators=(sysm.energyOp, sysm.meanSquaredRadiusOp), compat=True, accum=0))
     fk.init_ranlux(2)
     o.ranlux_tab[...] = fk.bufs[-2].reshape(o.ranlux_tab.shape)
     o.group_tab[...] = fk.bufs[-1].reshape(o.group_tab.shape)
-    p0 = sysm.initial_paths(W, N, np.random.RandomState(n)).astype(np.float32)
+    p0 = sysm.initial_paths(W, N, np.random.RandomState(n)).astype(np.float64 if double else np.float32)
     fk.set_paths(p0)
     o.paths[...] = p0.reshape(o.paths.shape)
     for _ in range(2):
